@@ -1,0 +1,1351 @@
+// C ABI of the GB300 HemoCell IB-LBM step: handle lifecycle, device memory,
+// stage orchestration (HemoCell::iterate, core/hemoCell.cpp:299-376), CUDA
+// graph replay for the batched form, readback and launch autotuning.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/hemocell_gb300.h"
+#include "hc_dev.h"
+#include "hc_host.h"
+
+using hcd::LbmView;
+using hcd::MechView;
+using hcd::TileGrid;
+using hcd::TypeDev;
+using hcd::VertexView;
+
+namespace {
+std::string g_create_error;
+
+struct TypeSlot {
+  std::string name;
+  hcg::TypeConstants tc;
+  hcg::ModelK k;
+  void* blob = nullptr;  // device arrays of this type
+  TypeDev dev;
+  int every = 1;
+  std::vector<int> cells;
+  int* dcells = nullptr;
+  int dcells_cap = 0;
+};
+}  // namespace
+
+struct hc_handle {
+  hc_params p;
+  hcg::Units u;
+  std::string err;
+  cudaStream_t stream = nullptr;
+  int nx = 0, ny = 0, nz = 0;
+  long long N = 0;
+  bool f64 = true;
+  size_t ts = 8;  // sizeof(T)
+  void* f[2] = {nullptr, nullptr};
+  void* F[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint32_t* nbmask = nullptr;
+  uint8_t* flag = nullptr;
+  void* bodyz = nullptr;
+  std::vector<uint8_t> hflag;
+  double uw[hcd::MAX_WALL_CLASSES][3];
+  int body_mode = 0;
+  double body[3] = {0, 0, 0};
+  // cells
+  std::vector<TypeSlot> types;
+  TypeDev* dtypes = nullptr;
+  long long Vcap = 0;
+  int nvert = 0;
+  double* x = nullptr;
+  void* v = nullptr;
+  void* fv = nullptr;
+  int* vcell = nullptr;
+  int* vnode = nullptr;
+  int* vtile = nullptr;
+  int cellcap = 0, ncells = 0;
+  int* cell_type = nullptr;
+  int* cell_voff = nullptr;
+  int* alive = nullptr;
+  int* dcells_all = nullptr;
+  std::vector<int> h_cell_type, h_cell_voff;
+  unsigned int* status = nullptr;
+  // binning
+  TileGrid tg;
+  int ntiles = 0;
+  int* bin_counts = nullptr;
+  int* bin_cursor = nullptr;
+  int* bin_offsets = nullptr;
+  int* tile_vertices = nullptr;
+  int* tile_cell_counts = nullptr;
+  int* tile_cell_offsets = nullptr;
+  int* tile_cells = nullptr;
+  long long bin_vcap = 0;
+  // stepping
+  int iter = 0;
+  int velocity_every = 1;
+  int tune[8] = {64, 4, 128, 128, 256, 0, 0, 0};  // k1 bx, k1 by, spread bs, ibm bs, mech bs, mech grid
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool graph_valid = false;
+  long long device_bytes = 0;
+  double* scratch = nullptr;  // readback staging
+  size_t scratch_bytes = 0;
+};
+
+namespace {
+
+#define HC_CUDA(h, call)                                                                        \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                           \
+      return HC_ERR_CUDA;                                                                      \
+    }                                                                                          \
+  } while (0)
+
+int fail(hc_handle* h, int code, const std::string& msg) {
+  h->err = msg;
+  return code;
+}
+
+cudaError_t dalloc(hc_handle* h, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) h->device_bytes += (long long)bytes;
+  return e;
+}
+
+void dfree(void* p) {
+  if (p) cudaFree(p);
+}
+
+void invalidate_graph(hc_handle* h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->graph[k]) {
+      cudaGraphExecDestroy(h->graph[k]);
+      h->graph[k] = nullptr;
+    }
+  h->graph_valid = false;
+}
+
+template <typename T>
+LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
+  LbmView<T> L;
+  L.nx = h->nx;
+  L.ny = h->ny;
+  L.nz = h->nz;
+  for (int a = 0; a < 3; ++a) L.per[a] = h->p.periodic[a];
+  L.N = h->N;
+  L.fsrc = (const T*)h->f[src];
+  L.fdst = (T*)h->f[1 - src];
+  L.Fcur = (const T*)h->F[fcur];
+  L.Fnext = (T*)h->F[1 - fcur];
+  L.nbmask = h->nbmask;
+  L.flag = h->flag;
+  L.bodyz = (const T*)h->bodyz;
+  L.omega = (T)(1.0 / h->u.tau);
+  for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
+    for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
+  return L;
+}
+
+template <typename T>
+VertexView<T> vertex_view(hc_handle* h) {
+  VertexView<T> vv;
+  vv.V = h->Vcap;
+  vv.nvert = h->nvert;
+  vv.x = h->x;
+  vv.v = (T*)h->v;
+  vv.f = (T*)h->fv;
+  vv.vcell = h->vcell;
+  vv.alive = h->alive;
+  vv.vnode = h->vnode;
+  vv.vtile = h->vtile;
+  vv.status = h->status;
+  return vv;
+}
+
+// ----- nbmask: per node, which directions bounce back and the wall class
+void build_nbmask(hc_handle* h, std::vector<uint32_t>& mask) {
+  static const int C[19][3] = {{0, 0, 0},  {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1},
+                               {-1, 0, 1}, {0, -1, -1}, {0, -1, 1}, {1, 0, 0}, {0, 1, 0},  {0, 0, 1},  {1, 1, 0},
+                               {1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {0, 1, 1}, {0, 1, -1}};
+  const int nx = h->nx, ny = h->ny, nz = h->nz;
+  mask.assign(h->N, 0);
+  for (int Z = 0; Z < nz; ++Z)
+    for (int Y = 0; Y < ny; ++Y)
+      for (int X = 0; X < nx; ++X) {
+        const long long n = X + (long long)nx * (Y + (long long)ny * Z);
+        if (h->hflag[n] != 0) {
+          mask[n] = hcd::NB_SOLID;
+          continue;
+        }
+        uint32_t m = 0;
+        int cls = -1;
+        bool mixed = false;
+        for (int i = 1; i < 19; ++i) {
+          int q[3] = {X + C[i][0], Y + C[i][1], Z + C[i][2]};
+          const int dims[3] = {nx, ny, nz};
+          bool out = false;
+          for (int a = 0; a < 3; ++a)
+            if (q[a] < 0 || q[a] >= dims[a]) {
+              if (h->p.periodic[a]) q[a] = (q[a] + dims[a]) % dims[a];
+              else out = true;
+            }
+          int c = -1;
+          if (out) c = 0;
+          else {
+            const uint8_t fl = h->hflag[q[0] + (long long)nx * (q[1] + (long long)ny * q[2])];
+            if (fl != 0) c = fl;
+          }
+          if (c >= 0) {
+            m |= 1u << (i - 1);
+            if (cls < 0) cls = c;
+            else if (cls != c) mixed = true;
+          }
+        }
+        uint32_t cw = cls < 0 ? 0u : (uint32_t)cls;
+        if (mixed || cw >= (uint32_t)hcd::MAX_WALL_CLASSES) cw = hcd::NB_CLASS_MIXED;
+        mask[n] = m | (cw << hcd::NB_CLASS_SHIFT);
+      }
+}
+
+int upload_flags(hc_handle* h) {
+  std::vector<uint32_t> mask;
+  build_nbmask(h, mask);
+  HC_CUDA(h, cudaMemcpyAsync(h->flag, h->hflag.data(), h->N, cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(h->nbmask, mask.data(), 4 * h->N, cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+template <typename T>
+__global__ void k_fill_body(T* F, const T* bodyz, long long plane, int nz, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int z = (int)(n / plane);
+  F[n] = bodyz[z];
+  F[N + n] = bodyz[nz + z];
+  F[2 * N + n] = bodyz[2 * nz + z];
+}
+
+template <typename T>
+__global__ void k_init_eq(T* f, const uint8_t* flag, long long N, double rho, double ux, double uy, double uz) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int C[19][3] = {{0, 0, 0},  {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1},
+                        {-1, 0, 1}, {0, -1, -1}, {0, -1, 1}, {1, 0, 0}, {0, 1, 0},  {0, 0, 1},  {1, 1, 0},
+                        {1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {0, 1, 1}, {0, 1, -1}};
+  const double uu = ux * ux + uy * uy + uz * uz;
+  for (int i = 0; i < 19; ++i) {
+    double w = i == 0 ? 1.0 / 3.0 : ((i - 1) % 9 < 3 ? 1.0 / 18.0 : 1.0 / 36.0);
+    double v = 0.0;
+    if (flag[n] == 0) {
+      const double cu = C[i][0] * ux + C[i][1] * uy + C[i][2] * uz;
+      v = w * ((rho - 1.0) + rho * (3.0 * cu + 4.5 * cu * cu - 1.5 * uu));
+    }
+    f[i * N + n] = (T)v;
+  }
+}
+
+int upload_body(hc_handle* h) {
+  std::vector<double> bz(3 * h->nz, 0.0);
+  for (int z = 0; z < h->nz; ++z) {
+    if (h->body_mode == HC_BODY_UNIFORM) {
+      for (int a = 0; a < 3; ++a) bz[a * h->nz + z] = h->body[a];
+    } else if (h->body_mode == HC_BODY_KOLMOGOROV) {
+      bz[z] = h->body[0] * std::sin(2.0 * M_PI * (double)z / (double)h->nz);
+    }
+  }
+  if (h->f64) {
+    HC_CUDA(h, cudaMemcpyAsync(h->bodyz, bz.data(), 8 * bz.size(), cudaMemcpyHostToDevice, h->stream));
+    k_fill_body<double><<<(unsigned)((h->N + 255) / 256), 256, 0, h->stream>>>(
+        (double*)h->F[h->cur], (const double*)h->bodyz, (long long)h->nx * h->ny, h->nz, h->N);
+  } else {
+    std::vector<float> bf(bz.begin(), bz.end());
+    HC_CUDA(h, cudaMemcpyAsync(h->bodyz, bf.data(), 4 * bf.size(), cudaMemcpyHostToDevice, h->stream));
+    k_fill_body<float><<<(unsigned)((h->N + 255) / 256), 256, 0, h->stream>>>(
+        (float*)h->F[h->cur], (const float*)h->bodyz, (long long)h->nx * h->ny, h->nz, h->N);
+  }
+  HC_CUDA(h, cudaGetLastError());
+  return HC_OK;
+}
+
+int ensure_scratch(hc_handle* h, size_t bytes) {
+  if (h->scratch_bytes >= bytes) return HC_OK;
+  if (h->scratch) {
+    cudaFree(h->scratch);
+    h->device_bytes -= (long long)h->scratch_bytes;
+  }
+  h->scratch = nullptr;
+  h->scratch_bytes = 0;
+  HC_CUDA(h, dalloc(h, (void**)&h->scratch, bytes));
+  h->scratch_bytes = bytes;
+  return HC_OK;
+}
+
+// grow a [3][V] SoA array from capacity oldV to newV
+int grow3(hc_handle* h, void** p, size_t es, long long oldV, long long newV, int nused) {
+  void* np = nullptr;
+  HC_CUDA(h, dalloc(h, &np, 3 * es * newV));
+  HC_CUDA(h, cudaMemsetAsync(np, 0, 3 * es * newV, h->stream));
+  if (*p && nused > 0)
+    for (int a = 0; a < 3; ++a)
+      HC_CUDA(h, cudaMemcpyAsync((char*)np + a * es * newV, (char*)*p + a * es * oldV, es * nused,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (*p) {
+    cudaFree(*p);
+    h->device_bytes -= (long long)(3 * es * oldV);
+  }
+  *p = np;
+  return HC_OK;
+}
+
+int grow1(hc_handle* h, void** p, size_t es, long long oldn, long long newn, long long nused) {
+  void* np = nullptr;
+  HC_CUDA(h, dalloc(h, &np, es * newn));
+  HC_CUDA(h, cudaMemsetAsync(np, 0, es * newn, h->stream));
+  if (*p && nused > 0) HC_CUDA(h, cudaMemcpyAsync(np, *p, es * nused, cudaMemcpyDeviceToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (*p) {
+    cudaFree(*p);
+    h->device_bytes -= (long long)(es * oldn);
+  }
+  *p = np;
+  return HC_OK;
+}
+
+int upload_types(hc_handle* h) {
+  std::vector<TypeDev> tv(hcd::MAX_TYPES);
+  for (size_t t = 0; t < h->types.size(); ++t) tv[t] = h->types[t].dev;
+  HC_CUDA(h, cudaMemcpyAsync(h->dtypes, tv.data(), sizeof(TypeDev) * hcd::MAX_TYPES, cudaMemcpyHostToDevice,
+                             h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+// per-type cell lists and the batched list (largest type first)
+int upload_cell_lists(hc_handle* h) {
+  for (TypeSlot& ts : h->types) {
+    if ((int)ts.cells.size() > ts.dcells_cap) {
+      dfree(ts.dcells);
+      ts.dcells_cap = std::max<int>((int)ts.cells.size(), 2 * ts.dcells_cap);
+      HC_CUDA(h, dalloc(h, (void**)&ts.dcells, sizeof(int) * ts.dcells_cap));
+    }
+    if (!ts.cells.empty())
+      HC_CUDA(h, cudaMemcpyAsync(ts.dcells, ts.cells.data(), sizeof(int) * ts.cells.size(), cudaMemcpyHostToDevice,
+                                 h->stream));
+  }
+  std::vector<int> order(h->types.size());
+  for (size_t t = 0; t < order.size(); ++t) order[t] = (int)t;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return h->types[a].tc.nv > h->types[b].tc.nv; });
+  std::vector<int> all;
+  for (int t : order) all.insert(all.end(), h->types[t].cells.begin(), h->types[t].cells.end());
+  if (!all.empty())
+    HC_CUDA(h, cudaMemcpyAsync(h->dcells_all, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+// ----- stage launchers (enqueue only) -------------------------------------
+template <typename T>
+int enq_spread(hc_handle* h) {
+  LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
+  HC_CUDA(h, hcd::launch_spread<T>(L, vertex_view<T>(h), h->u.f_limit, h->tune[2], h->stream));
+  return HC_OK;
+}
+
+template <typename T>
+int enq_collide(hc_handle* h) {
+  LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
+  HC_CUDA(h, hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream));
+  h->cur ^= 1;
+  return HC_OK;
+}
+
+// post-stream view: populations f[cur], force of the last collision F[1-cur]
+template <typename T>
+int enq_interp_advance(hc_handle* h, int do_interp, int do_advance) {
+  LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
+  HC_CUDA(h, hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, do_interp, do_advance, h->tune[3],
+                                           h->stream));
+  return HC_OK;
+}
+
+template <typename T>
+int enq_mechanics(hc_handle* h, bool forced) {
+  bool all_due = true;
+  for (TypeSlot& ts : h->types)
+    if (!(forced || h->iter % ts.every == 0)) all_due = false;
+  MechView<T> M;
+  M.cell_type = h->cell_type;
+  M.cell_voff = h->cell_voff;
+  M.types = h->dtypes;
+  M.vv = vertex_view<T>(h);
+  if (h->p.launch == HC_LAUNCH_BATCHED && all_due && h->ncells > 0) {
+    int maxnv = 0;
+    for (TypeSlot& ts : h->types)
+      if (!ts.cells.empty()) maxnv = std::max(maxnv, ts.tc.nv);
+    M.cells = h->dcells_all;
+    M.ncells = h->ncells;
+    M.dyn_smem = (int)hcd::mechanics_smem_bytes<T>(maxnv);
+    HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], h->tune[5], h->stream));
+    return HC_OK;
+  }
+  for (TypeSlot& ts : h->types) {
+    if (ts.cells.empty() || !(forced || h->iter % ts.every == 0)) continue;
+    M.cells = ts.dcells;
+    M.ncells = (int)ts.cells.size();
+    M.dyn_smem = (int)hcd::mechanics_smem_bytes<T>(ts.tc.nv);
+    HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], 0, h->stream));
+  }
+  return HC_OK;
+}
+
+// one HemoCell::iterate(): spread, collide+stream (+force reset), interpolate
+// (every velocity_every), advance, constitutive model (due types).
+template <typename T>
+int enq_step(hc_handle* h) {
+  int rc;
+  if ((rc = enq_spread<T>(h)) != HC_OK) return rc;
+  if ((rc = enq_collide<T>(h)) != HC_OK) return rc;
+  if ((rc = enq_interp_advance<T>(h, h->iter % h->velocity_every == 0, 1)) != HC_OK) return rc;
+  if ((rc = enq_mechanics<T>(h, false)) != HC_OK) return rc;
+  h->iter++;
+  return HC_OK;
+}
+
+bool graph_eligible(hc_handle* h) {
+  if (h->p.launch != HC_LAUNCH_BATCHED) return false;
+  if (h->velocity_every != 1) return false;
+  for (TypeSlot& ts : h->types)
+    if (ts.every != 1) return false;
+  return true;
+}
+
+template <typename T>
+int build_graph(hc_handle* h, int parity) {
+  const int save_cur = h->cur, save_iter = h->iter;
+  h->cur = parity;
+  cudaGraph_t g = nullptr;
+  HC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enq_step<T>(h);
+  if (rc == HC_OK) rc = enq_step<T>(h);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  h->cur = save_cur;
+  h->iter = save_iter;
+  if (rc != HC_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(h, HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph[parity], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(h, HC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return HC_OK;
+}
+
+template <typename T>
+int run_steps(hc_handle* h, int nsteps) {
+  int rc;
+  if (graph_eligible(h) && nsteps >= 2) {
+    if (!h->graph_valid) {
+      invalidate_graph(h);
+      if ((rc = build_graph<T>(h, 0)) != HC_OK) return rc;
+      if ((rc = build_graph<T>(h, 1)) != HC_OK) return rc;
+      h->graph_valid = true;
+    }
+    while (nsteps >= 2) {
+      HC_CUDA(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+      h->iter += 2;
+      nsteps -= 2;
+    }
+  }
+  for (int k = 0; k < nsteps; ++k)
+    if ((rc = enq_step<T>(h)) != HC_OK) return rc;
+  return HC_OK;
+}
+
+template <typename T>
+int run_stage(hc_handle* h, int stage) {
+  switch (stage) {
+    case HC_STAGE_SPREAD:
+      return enq_spread<T>(h);
+    case HC_STAGE_COLLIDE_STREAM:
+      return enq_collide<T>(h);
+    case HC_STAGE_INTERPOLATE:
+      return enq_interp_advance<T>(h, 1, 0);
+    case HC_STAGE_ADVANCE:
+      return enq_interp_advance<T>(h, 0, 1);
+    case HC_STAGE_MECHANICS:
+      return enq_mechanics<T>(h, false);
+    case HC_STAGE_MECHANICS_FORCED:
+      return enq_mechanics<T>(h, true);
+    case HC_STAGE_BIN: {
+      LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
+      HC_CUDA(h, hcd::launch_bin_vertices<T>(L, vertex_view<T>(h), h->tg, h->stream));
+      if (h->bin_vcap < h->Vcap || !h->bin_counts) {
+        dfree(h->tile_vertices);
+        dfree(h->tile_cells);
+        HC_CUDA(h, dalloc(h, (void**)&h->tile_vertices, sizeof(int) * std::max<long long>(1, h->Vcap)));
+        HC_CUDA(h, dalloc(h, (void**)&h->tile_cells, sizeof(int) * std::max<long long>(1, h->Vcap)));
+        h->bin_vcap = h->Vcap;
+      }
+      if (!h->bin_counts) {
+        const int nt = h->ntiles;
+        HC_CUDA(h, dalloc(h, (void**)&h->bin_counts, sizeof(int) * nt));
+        HC_CUDA(h, dalloc(h, (void**)&h->bin_cursor, sizeof(int) * nt));
+        HC_CUDA(h, dalloc(h, (void**)&h->bin_offsets, sizeof(int) * (nt + 1)));
+        HC_CUDA(h, dalloc(h, (void**)&h->tile_cell_counts, sizeof(int) * nt));
+        HC_CUDA(h, dalloc(h, (void**)&h->tile_cell_offsets, sizeof(int) * (nt + 1)));
+      }
+      HC_CUDA(h, hcd::launch_bin_csr(h->vtile, h->nvert, h->ntiles, h->bin_counts, h->bin_offsets, h->bin_cursor,
+                                     h->tile_vertices, h->vcell, h->tile_cell_counts, h->stream));
+      HC_CUDA(h, hcd::launch_tile_cells(h->bin_offsets, h->tile_vertices, h->vcell, h->ntiles, h->tile_cell_counts,
+                                        h->tile_cell_offsets, h->tile_cells, (int)h->bin_vcap, h->stream));
+      return HC_OK;
+    }
+    default:
+      return fail(h, HC_ERR_INVALID, "unknown stage");
+  }
+}
+
+int add_cells_positions(hc_handle* h, int type, int n, const std::vector<double>& xyz) {
+  TypeSlot& ts = h->types[type];
+  const int nv = ts.tc.nv;
+  const long long need = (long long)h->nvert + (long long)n * nv;
+  if (need > (long long)INT32_MAX / 4) return fail(h, HC_ERR_INVALID, "too many vertices");
+  for (double q : xyz)
+    if (!std::isfinite(q)) return fail(h, HC_ERR_NUMERIC, "non-finite vertex position");
+  invalidate_graph(h);
+  int rc;
+  if (need > h->Vcap) {
+    long long nc = std::max<long long>(need, 2 * h->Vcap);
+    nc = std::max<long long>(nc, 1024);
+    if ((rc = grow3(h, (void**)&h->x, 8, h->Vcap, nc, h->nvert)) != HC_OK) return rc;
+    if ((rc = grow3(h, &h->v, h->ts, h->Vcap, nc, h->nvert)) != HC_OK) return rc;
+    if ((rc = grow3(h, &h->fv, h->ts, h->Vcap, nc, h->nvert)) != HC_OK) return rc;
+    if ((rc = grow1(h, (void**)&h->vcell, 4, h->Vcap, nc, h->nvert)) != HC_OK) return rc;
+    if ((rc = grow1(h, (void**)&h->vnode, 4, h->Vcap, nc, h->nvert)) != HC_OK) return rc;
+    if ((rc = grow1(h, (void**)&h->vtile, 4, h->Vcap, nc, h->nvert)) != HC_OK) return rc;
+    h->Vcap = nc;
+  }
+  const int needc = h->ncells + n;
+  if (needc > h->cellcap) {
+    int nc = std::max(needc, std::max(2 * h->cellcap, 64));
+    if ((rc = grow1(h, (void**)&h->cell_type, 4, h->cellcap, nc, h->ncells)) != HC_OK) return rc;
+    if ((rc = grow1(h, (void**)&h->cell_voff, 4, h->cellcap, nc, h->ncells)) != HC_OK) return rc;
+    if ((rc = grow1(h, (void**)&h->alive, 4, h->cellcap, nc, h->ncells)) != HC_OK) return rc;
+    if ((rc = grow1(h, (void**)&h->dcells_all, 4, h->cellcap, nc, h->ncells)) != HC_OK) return rc;
+    h->cellcap = nc;
+  }
+  // positions: host layout [V][3] -> device [3][Vcap]
+  const int first = h->ncells;
+  std::vector<double> comp(n * (size_t)nv);
+  for (int a = 0; a < 3; ++a) {
+    for (size_t k = 0; k < comp.size(); ++k) comp[k] = xyz[3 * k + a];
+    HC_CUDA(h, cudaMemcpyAsync(h->x + a * h->Vcap + h->nvert, comp.data(), 8 * comp.size(), cudaMemcpyHostToDevice,
+                               h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  std::vector<int> vc(n * (size_t)nv), ct(n), co(n), al(n, 1);
+  for (int c = 0; c < n; ++c) {
+    ct[c] = type;
+    co[c] = h->nvert + c * nv;
+    for (int k = 0; k < nv; ++k) vc[(size_t)c * nv + k] = first + c;
+    h->h_cell_type.push_back(type);
+    h->h_cell_voff.push_back(co[c]);
+    ts.cells.push_back(first + c);
+  }
+  HC_CUDA(h, cudaMemcpyAsync(h->vcell + h->nvert, vc.data(), 4 * vc.size(), cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(h->cell_type + first, ct.data(), 4 * n, cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(h->cell_voff + first, co.data(), 4 * n, cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(h->alive + first, al.data(), 4 * n, cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->nvert += n * nv;
+  h->ncells += n;
+  return upload_cell_lists(h);
+}
+
+template <typename T>
+__global__ void k_soa_to_aos(const T* src, double* dst, long long V, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[3 * (long long)i] = (double)src[i];
+  dst[3 * (long long)i + 1] = (double)src[V + i];
+  dst[3 * (long long)i + 2] = (double)src[2 * V + i];
+}
+
+// device [3][Vcap] (T) -> host [V][3] double: transpose on the device, then
+// one D2H copy straight into the caller's buffer
+template <typename T>
+int read3(hc_handle* h, const void* src, double* out) {
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 3 * std::max<int>(1, h->nvert))) != HC_OK) return rc;
+  k_soa_to_aos<T><<<(h->nvert + 255) / 256, 256, 0, h->stream>>>((const T*)src, h->scratch, h->Vcap, h->nvert);
+  HC_CUDA(h, cudaGetLastError());
+  HC_CUDA(h, cudaMemcpyAsync(out, h->scratch, 8 * 3 * (size_t)h->nvert, cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int write3(hc_handle* h, void* dst, size_t es, const double* in) {
+  const long long V = h->Vcap;
+  std::vector<double> buf(3 * V, 0.0);
+  for (int i = 0; i < h->nvert; ++i)
+    for (int a = 0; a < 3; ++a) buf[a * V + i] = in[3 * i + a];
+  if (es == 8) {
+    HC_CUDA(h, cudaMemcpyAsync(dst, buf.data(), 8 * 3 * V, cudaMemcpyHostToDevice, h->stream));
+  } else {
+    int rc;
+    if ((rc = ensure_scratch(h, sizeof(double) * 3 * V)) != HC_OK) return rc;
+    HC_CUDA(h, cudaMemcpyAsync(h->scratch, buf.data(), 8 * 3 * V, cudaMemcpyHostToDevice, h->stream));
+    HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)dst, 3 * V, 0.0, 1, h->stream));
+  }
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+// ----- autotuner: time candidate launch shapes on the live state --------
+template <typename T>
+float time_it(hc_handle* h, int reps, int which) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  auto once = [&]() {
+    if (which == 0) {
+      LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
+      hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream);
+    } else if (which == 1) {
+      LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
+      hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, 1, 0, h->tune[3], h->stream);
+    } else {
+      enq_mechanics<T>(h, true);
+    }
+  };
+  once();
+  cudaEventRecord(a, h->stream);
+  for (int r = 0; r < reps; ++r) once();
+  cudaEventRecord(b, h->stream);
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (cudaGetLastError() != cudaSuccess) return 1e30f;
+  return ms / reps;
+}
+
+std::string tune_key(hc_handle* h) {
+  std::ostringstream k;
+  k << (h->f64 ? "f64" : "f32") << "_" << h->nx << "x" << h->ny << "x" << h->nz << "_V" << h->nvert << "_C"
+    << h->ncells << "_L" << h->p.launch;
+  return k.str();
+}
+
+template <typename T>
+int autotune(hc_handle* h, const char* cache) {
+  const std::string key = tune_key(h);
+  if (cache && *cache) {
+    std::ifstream in(cache);
+    std::string k;
+    int t[8];
+    while (in >> k >> t[0] >> t[1] >> t[2] >> t[3] >> t[4] >> t[5] >> t[6] >> t[7])
+      if (k == key) {
+        std::memcpy(h->tune, t, sizeof(t));
+        invalidate_graph(h);
+        return HC_OK;
+      }
+  }
+  // state that the candidates overwrite: the f[1-cur], F[1-cur] buffers are
+  // rewritten by the next step anyway; vertex v and force are saved.
+  const size_t vb = 3 * h->ts * (size_t)h->Vcap;
+  void *sv = nullptr, *sf = nullptr;
+  if (h->Vcap > 0) {
+    HC_CUDA(h, cudaMalloc(&sv, vb));
+    HC_CUDA(h, cudaMalloc(&sf, vb));
+    HC_CUDA(h, cudaMemcpyAsync(sv, h->v, vb, cudaMemcpyDeviceToDevice, h->stream));
+    HC_CUDA(h, cudaMemcpyAsync(sf, h->fv, vb, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  const int k1[][2] = {{32, 4}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {256, 1}, {32, 8}};
+  float best = 1e30f;
+  int bx = h->tune[0], by = h->tune[1];
+  for (auto& c : k1) {
+    if (c[0] > 2 * h->nx && c[0] > 32) continue;
+    h->tune[0] = c[0];
+    h->tune[1] = c[1];
+    float t = time_it<T>(h, 5, 0);
+    if (t < best) {
+      best = t;
+      bx = c[0];
+      by = c[1];
+    }
+  }
+  h->tune[0] = bx;
+  h->tune[1] = by;
+  if (h->nvert > 0) {
+    best = 1e30f;
+    int bb = h->tune[3];
+    for (int bs : {64, 128, 256}) {
+      h->tune[3] = bs;
+      float t = time_it<T>(h, 5, 1);
+      if (t < best) {
+        best = t;
+        bb = bs;
+      }
+    }
+    h->tune[3] = bb;
+    h->tune[2] = bb;
+    best = 1e30f;
+    int mb = h->tune[4], mg = h->tune[5];
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
+    for (int bs : {128, 256, 512})
+      for (int gr : {0, 2 * sms, 4 * sms}) {
+        if (gr != 0 && h->p.launch != HC_LAUNCH_BATCHED) continue;
+        h->tune[4] = bs;
+        h->tune[5] = gr;
+        float t = time_it<T>(h, 3, 2);
+        if (t < best) {
+          best = t;
+          mb = bs;
+          mg = gr;
+        }
+      }
+    h->tune[4] = mb;
+    h->tune[5] = mg;
+    HC_CUDA(h, cudaMemcpyAsync(h->v, sv, vb, cudaMemcpyDeviceToDevice, h->stream));
+    HC_CUDA(h, cudaMemcpyAsync(h->fv, sf, vb, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (sv) cudaFree(sv);
+  if (sf) cudaFree(sf);
+  invalidate_graph(h);
+  if (cache && *cache) {
+    std::ofstream out(cache, std::ios::app);
+    out << key;
+    for (int k = 0; k < 8; ++k) out << " " << h->tune[k];
+    out << "\n";
+  }
+  return HC_OK;
+}
+
+template <typename T>
+int profile_stages(hc_handle* h, int nsteps, double* out) {
+  cudaEvent_t ev[5];
+  for (auto& e : ev) HC_CUDA(h, cudaEventCreate(&e));
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (int k = 0; k < nsteps; ++k) {
+    int rc;
+    HC_CUDA(h, cudaEventRecord(ev[0], h->stream));
+    if ((rc = enq_spread<T>(h)) != HC_OK) return rc;
+    HC_CUDA(h, cudaEventRecord(ev[1], h->stream));
+    if ((rc = enq_collide<T>(h)) != HC_OK) return rc;
+    HC_CUDA(h, cudaEventRecord(ev[2], h->stream));
+    if ((rc = enq_interp_advance<T>(h, h->iter % h->velocity_every == 0, 1)) != HC_OK) return rc;
+    HC_CUDA(h, cudaEventRecord(ev[3], h->stream));
+    if ((rc = enq_mechanics<T>(h, false)) != HC_OK) return rc;
+    HC_CUDA(h, cudaEventRecord(ev[4], h->stream));
+    h->iter++;
+    HC_CUDA(h, cudaEventSynchronize(ev[4]));
+    float t;
+    for (int s = 0; s < 4; ++s) {
+      HC_CUDA(h, cudaEventElapsedTime(&t, ev[s], ev[s + 1]));
+      acc[s] += t;
+    }
+    HC_CUDA(h, cudaEventElapsedTime(&t, ev[0], ev[4]));
+    acc[4] += t;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  for (int s = 0; s < 5; ++s) out[s] = nsteps > 0 ? acc[s] / nsteps : 0.0;
+  return HC_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+hc_handle* hc_create(const hc_params* p) {
+  g_create_error.clear();
+  if (!p) {
+    g_create_error = "null params";
+    return nullptr;
+  }
+  if (p->nx <= 0 || p->ny <= 0 || p->nz <= 0) {
+    g_create_error = "lattice dimensions must be positive";
+    return nullptr;
+  }
+  if ((long long)p->nx * p->ny * p->nz * 19 >= (1LL << 31) * 4) {
+    g_create_error = "lattice too large";
+    return nullptr;
+  }
+  if (!(p->dx > 0) || !(p->dt > 0) || !(p->rho_p > 0)) {
+    g_create_error = "dx, dt and rhoP must be positive";
+    return nullptr;
+  }
+  if (p->form != HC_FORM_PLAIN_F64 && p->form != HC_FORM_MIXED_F32) {
+    g_create_error = "unknown precision form";
+    return nullptr;
+  }
+  if (p->launch != HC_LAUNCH_PER_STAGE && p->launch != HC_LAUNCH_BATCHED) {
+    g_create_error = "unknown launch mode";
+    return nullptr;
+  }
+  hcg::Units u = hcg::derive_units(p->dx, p->dt, p->nu_p, p->rho_p, p->kBT_p, p->tau);
+  if (!(u.tau > 0.5)) {
+    // core/hemoCell.cpp sanityCheck: tau must exceed 1/2 for a positive viscosity
+    g_create_error = "tau must be > 0.5";
+    return nullptr;
+  }
+  hc_handle* h = new hc_handle();
+  h->p = *p;
+  h->u = u;
+  std::memset(h->uw, 0, sizeof(h->uw));
+  h->nx = p->nx;
+  h->ny = p->ny;
+  h->nz = p->nz;
+  h->N = (long long)p->nx * p->ny * p->nz;
+  h->f64 = p->form == HC_FORM_PLAIN_F64;
+  h->ts = h->f64 ? 8 : 4;
+  h->tg.tx = p->tile[0] > 0 ? p->tile[0] : 8;
+  h->tg.ty = p->tile[1] > 0 ? p->tile[1] : 8;
+  h->tg.tz = p->tile[2] > 0 ? p->tile[2] : 8;
+  h->tg.ntx = (h->nx + h->tg.tx - 1) / h->tg.tx;
+  h->tg.nty = (h->ny + h->tg.ty - 1) / h->tg.ty;
+  h->tg.ntz = (h->nz + h->tg.tz - 1) / h->tg.tz;
+  h->ntiles = h->tg.ntx * h->tg.nty * h->tg.ntz;
+  auto bail = [&](const std::string& m) {
+    g_create_error = m;
+    hc_destroy(h);
+    return (hc_handle*)nullptr;
+  };
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e != cudaSuccess) return bail(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(std::string("stream: ") + cudaGetErrorString(e));
+  const size_t fb = 19 * h->ts * (size_t)h->N, Fb = 3 * h->ts * (size_t)h->N;
+  for (int k = 0; k < 2; ++k) {
+    if ((e = dalloc(h, &h->f[k], fb)) != cudaSuccess) return bail("out of device memory (populations)");
+    if ((e = dalloc(h, &h->F[k], Fb)) != cudaSuccess) return bail("out of device memory (force field)");
+    cudaMemsetAsync(h->f[k], 0, fb, h->stream);
+    cudaMemsetAsync(h->F[k], 0, Fb, h->stream);
+  }
+  if (dalloc(h, (void**)&h->nbmask, 4 * h->N) != cudaSuccess || dalloc(h, (void**)&h->flag, h->N) != cudaSuccess ||
+      dalloc(h, &h->bodyz, 3 * h->ts * h->nz) != cudaSuccess ||
+      dalloc(h, (void**)&h->dtypes, sizeof(TypeDev) * hcd::MAX_TYPES) != cudaSuccess ||
+      dalloc(h, (void**)&h->status, sizeof(unsigned int)) != cudaSuccess)
+    return bail("out of device memory");
+  cudaMemsetAsync(h->bodyz, 0, 3 * h->ts * h->nz, h->stream);
+  cudaMemsetAsync(h->status, 0, sizeof(unsigned int), h->stream);
+  h->hflag.assign(h->N, 0);
+  if (upload_flags(h) != HC_OK) return bail(h->err);
+  if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(cudaGetErrorString(e));
+  return h;
+}
+
+int hc_destroy(hc_handle* h) {
+  if (!h) return HC_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  invalidate_graph(h);
+  for (int k = 0; k < 2; ++k) {
+    dfree(h->f[k]);
+    dfree(h->F[k]);
+  }
+  for (TypeSlot& ts : h->types) {
+    dfree(ts.blob);
+    dfree(ts.dcells);
+  }
+  void* ptrs[] = {h->nbmask, h->flag,  h->bodyz,     h->dtypes,     h->x,          h->v,
+                  h->fv,     h->vcell, h->vnode,     h->vtile,      h->cell_type,  h->cell_voff,
+                  h->alive,  h->dcells_all, h->status, h->bin_counts, h->bin_cursor, h->bin_offsets,
+                  h->tile_vertices, h->tile_cell_counts, h->tile_cell_offsets, h->tile_cells, h->scratch};
+  for (void* q : ptrs) dfree(q);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return HC_OK;
+}
+
+const char* hc_last_error(const hc_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int hc_derived_units(const hc_handle* h, double* out) {
+  if (!h || !out) return HC_ERR_INVALID;
+  out[0] = h->u.tau;
+  out[1] = h->u.nu_lbm;
+  out[2] = h->u.dm;
+  out[3] = h->u.df;
+  out[4] = h->u.kBT_lbm;
+  out[5] = h->u.f_limit;
+  return HC_OK;
+}
+
+int hc_set_flags(hc_handle* h, const uint8_t* flags) {
+  if (!h || !flags) return HC_ERR_INVALID;
+  std::memcpy(h->hflag.data(), flags, h->N);
+  invalidate_graph(h);
+  return upload_flags(h);
+}
+
+int hc_set_wall_velocity(hc_handle* h, int cls, const double* u3) {
+  if (!h || !u3) return HC_ERR_INVALID;
+  if (cls < 0 || cls >= hcd::MAX_WALL_CLASSES) return fail(h, HC_ERR_INVALID, "wall class out of range [0,16)");
+  for (int a = 0; a < 3; ++a) h->uw[cls][a] = u3[a];
+  invalidate_graph(h);
+  return HC_OK;
+}
+
+int hc_set_body_force(hc_handle* h, int mode, const double* p) {
+  if (!h) return HC_ERR_INVALID;
+  if (mode < HC_BODY_NONE || mode > HC_BODY_KOLMOGOROV) return fail(h, HC_ERR_INVALID, "unknown body-force mode");
+  if (mode != HC_BODY_NONE && !p) return fail(h, HC_ERR_INVALID, "body-force parameters missing");
+  h->body_mode = mode;
+  for (int a = 0; a < 3; ++a) h->body[a] = (mode != HC_BODY_NONE) ? p[a] : 0.0;
+  if (mode == HC_BODY_KOLMOGOROV) h->body[1] = h->body[2] = 0.0;
+  return upload_body(h);
+}
+
+int hc_init_equilibrium(hc_handle* h, double rho, const double* u3) {
+  if (!h) return HC_ERR_INVALID;
+  if (!(rho > 0)) return fail(h, HC_ERR_INVALID, "density must be positive");
+  const double ux = u3 ? u3[0] : 0, uy = u3 ? u3[1] : 0, uz = u3 ? u3[2] : 0;
+  const unsigned g = (unsigned)((h->N + 255) / 256);
+  if (h->f64) k_init_eq<double><<<g, 256, 0, h->stream>>>((double*)h->f[h->cur], h->flag, h->N, rho, ux, uy, uz);
+  else k_init_eq<float><<<g, 256, 0, h->stream>>>((float*)h->f[h->cur], h->flag, h->N, rho, ux, uy, uz);
+  HC_CUDA(h, cudaGetLastError());
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_material* m, const double* xyz, int nv,
+                     const int* tris, int nf, const int* inner, int ni) {
+  if (!h || !m || !xyz || !tris) return HC_ERR_INVALID;
+  if ((int)h->types.size() >= hcd::MAX_TYPES) return fail(h, HC_ERR_INVALID, "more than 8 cell types");
+  if (model < HC_MODEL_RBC_HIGH_ORDER || model > HC_MODEL_WBC_HIGH_ORDER)
+    return fail(h, HC_ERR_INVALID, "unknown constitutive model");
+  if (nv <= 0 || nf <= 0 || ni < 0 || (ni > 0 && !inner)) return fail(h, HC_ERR_INVALID, "bad mesh sizes");
+  if (nv > 65535) return fail(h, HC_ERR_INVALID, "more vertices per cell than UINT16_MAX");
+  TypeSlot ts;
+  ts.name = name ? name : "";
+  std::vector<hcg::Vec3> P(nv);
+  for (int i = 0; i < nv; ++i) P[i] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  std::vector<std::array<int, 3>> T(nf);
+  for (int k = 0; k < nf; ++k) T[k] = {tris[3 * k], tris[3 * k + 1], tris[3 * k + 2]};
+  std::vector<std::array<int, 2>> I(ni);
+  for (int k = 0; k < ni; ++k) I[k] = {inner[2 * k], inner[2 * k + 1]};
+  std::string why = hcg::build_constants(ts.tc, model, P, T, I);
+  if (!why.empty()) return fail(h, HC_ERR_INVALID, "cell type " + ts.name + ": " + why);
+  const double mat[9] = {m->kLink, m->kBend, m->kVolume, m->kArea, m->eta_m,
+                         m->kInnerRigid, m->kCytoskeleton, m->coreRadius, m->radius};
+  ts.k = hcg::scale_material(model, nf, h->u, h->p.dx, h->p.dt, mat);
+  const size_t smem = (h->f64 ? hcd::mechanics_smem_bytes<double>(nv) : hcd::mechanics_smem_bytes<float>(nv));
+  if (smem > 227 * 1024) return fail(h, HC_ERR_INVALID, "cell type too large for one CTA's shared memory");
+  {
+    size_t need = smem;
+    for (TypeSlot& o : h->types)
+      need = std::max(need, h->f64 ? hcd::mechanics_smem_bytes<double>(o.tc.nv) : hcd::mechanics_smem_bytes<float>(o.tc.nv));
+    HC_CUDA(h, h->f64 ? hcd::prepare_mechanics<double>((int)need) : hcd::prepare_mechanics<float>((int)need));
+  }
+  // one device blob: ints then doubles
+  const hcg::TypeConstants& c = ts.tc;
+  std::vector<int> iv;
+  auto put_i = [&](const std::vector<int>& a) {
+    size_t o = iv.size();
+    iv.insert(iv.end(), a.begin(), a.end());
+    return o;
+  };
+  const size_t o_tris = put_i(c.tris), o_edges = put_i(c.edges), o_bt = put_i(c.bend_tris),
+               o_bo = put_i(c.bend_outer), o_ring = put_i(c.ring), o_rn = put_i(c.ring_n), o_in = put_i(c.inner);
+  while (iv.size() % 2) iv.push_back(0);
+  std::vector<double> dv;
+  auto put_d = [&](const std::vector<double>& a) {
+    size_t o = dv.size();
+    dv.insert(dv.end(), a.begin(), a.end());
+    return o;
+  };
+  const size_t o_a0 = put_d(c.tri_a0), o_l0 = put_d(c.edge_l0), o_ang = put_d(c.edge_angle0),
+               o_pd = put_d(c.patch_d0), o_il = put_d(c.inner_l0);
+  const size_t ib = 4 * iv.size(), db = 8 * std::max<size_t>(dv.size(), 1);
+  HC_CUDA(h, dalloc(h, &ts.blob, ib + db));
+  HC_CUDA(h, cudaMemcpy(ts.blob, iv.data(), ib, cudaMemcpyHostToDevice));
+  if (!dv.empty()) HC_CUDA(h, cudaMemcpy((char*)ts.blob + ib, dv.data(), 8 * dv.size(), cudaMemcpyHostToDevice));
+  const int* ibase = (const int*)ts.blob;
+  const double* dbase = (const double*)((char*)ts.blob + ib);
+  TypeDev& d = ts.dev;
+  d.model = model;
+  d.nv = c.nv;
+  d.nf = c.nf;
+  d.ne = c.ne;
+  d.ni = c.ni;
+  d.tris = ibase + o_tris;
+  d.edges = ibase + o_edges;
+  d.bend_tris = ibase + o_bt;
+  d.bend_outer = ibase + o_bo;
+  d.ring = ibase + o_ring;
+  d.ring_n = ibase + o_rn;
+  d.inner = ibase + o_in;
+  d.tri_a0 = dbase + o_a0;
+  d.edge_l0 = dbase + o_l0;
+  d.edge_angle0 = dbase + o_ang;
+  d.patch_d0 = dbase + o_pd;
+  d.inner_l0 = dbase + o_il;
+  d.volume_eq = c.volume_eq;
+  d.area_mean_eq = c.area_mean_eq;
+  d.edge_mean_eq = c.edge_mean_eq;
+  d.k_link = ts.k.k_link;
+  d.k_bend = ts.k.k_bend;
+  d.k_volume = ts.k.k_volume;
+  d.k_area = ts.k.k_area;
+  d.eta_m = ts.k.eta_m;
+  d.k_inner_rigid = ts.k.k_inner_rigid;
+  d.k_cyto = ts.k.k_cyto;
+  d.core_radius = ts.k.core_radius;
+  d.radius = ts.k.radius;
+  h->types.push_back(std::move(ts));
+  invalidate_graph(h);
+  int rc = upload_types(h);
+  if (rc != HC_OK) return rc;
+  return (int)h->types.size() - 1;
+}
+
+int hc_add_cells(hc_handle* h, int type, int n, const double* centres, const double* angles) {
+  if (!h || n < 0 || (n > 0 && (!centres || !angles))) return HC_ERR_INVALID;
+  if (type < 0 || type >= (int)h->types.size()) return fail(h, HC_ERR_INVALID, "unknown cell type");
+  std::vector<double> xyz;
+  xyz.reserve(3 * (size_t)n * h->types[type].tc.nv);
+  for (int c = 0; c < n; ++c) hcg::place_cell(h->types[type].tc.rest, centres + 3 * c, angles + 3 * c, xyz);
+  const int first = h->ncells;
+  int rc = add_cells_positions(h, type, n, xyz);
+  return rc == HC_OK ? first : rc;
+}
+
+int hc_add_cells_xyz(hc_handle* h, int type, int n, const double* xyz) {
+  if (!h || n < 0 || (n > 0 && !xyz)) return HC_ERR_INVALID;
+  if (type < 0 || type >= (int)h->types.size()) return fail(h, HC_ERR_INVALID, "unknown cell type");
+  std::vector<double> v(xyz, xyz + 3 * (size_t)n * h->types[type].tc.nv);
+  const int first = h->ncells;
+  int rc = add_cells_positions(h, type, n, v);
+  return rc == HC_OK ? first : rc;
+}
+
+int hc_set_timescales(hc_handle* h, const int* every, int ntypes, int velocity_every) {
+  if (!h) return HC_ERR_INVALID;
+  if (velocity_every < 1) return fail(h, HC_ERR_INVALID, "velocity timescale must be >= 1");
+  if (ntypes != (int)h->types.size() || (ntypes > 0 && !every))
+    return fail(h, HC_ERR_INVALID, "one material timescale per cell type is required");
+  for (int t = 0; t < ntypes; ++t) {
+    if (every[t] < 1) return fail(h, HC_ERR_INVALID, "material timescale must be >= 1");
+    // core/hemoCell.cpp:620-627
+    if (every[t] % velocity_every != 0)
+      return fail(h, HC_ERR_INVALID, "velocity timescale separation cannot divide all material timescale separations");
+  }
+  for (int t = 0; t < ntypes; ++t) h->types[t].every = every[t];
+  h->velocity_every = velocity_every;
+  invalidate_graph(h);
+  return HC_OK;
+}
+
+int hc_step(hc_handle* h, int nsteps) {
+  if (!h || nsteps < 0) return HC_ERR_INVALID;
+  return h->f64 ? run_steps<double>(h, nsteps) : run_steps<float>(h, nsteps);
+}
+
+int hc_stage(hc_handle* h, int stage) {
+  if (!h) return HC_ERR_INVALID;
+  return h->f64 ? run_stage<double>(h, stage) : run_stage<float>(h, stage);
+}
+
+int hc_sync(hc_handle* h) {
+  if (!h) return HC_ERR_INVALID;
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_time_steps(hc_handle* h, int nsteps, double* ms) {
+  if (!h || !ms || nsteps < 0) return HC_ERR_INVALID;
+  cudaEvent_t a, b;
+  HC_CUDA(h, cudaEventCreate(&a));
+  HC_CUDA(h, cudaEventCreate(&b));
+  HC_CUDA(h, cudaEventRecord(a, h->stream));
+  int rc = h->f64 ? run_steps<double>(h, nsteps) : run_steps<float>(h, nsteps);
+  HC_CUDA(h, cudaEventRecord(b, h->stream));
+  HC_CUDA(h, cudaEventSynchronize(b));
+  float t = 0;
+  HC_CUDA(h, cudaEventElapsedTime(&t, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms = t;
+  return rc;
+}
+
+int hc_profile_stages(hc_handle* h, int nsteps, double* ms5) {
+  if (!h || !ms5 || nsteps < 0) return HC_ERR_INVALID;
+  return h->f64 ? profile_stages<double>(h, nsteps, ms5) : profile_stages<float>(h, nsteps, ms5);
+}
+
+int hc_read_fluid(hc_handle* h, double* rho, double* u) {
+  if (!h) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 4 * h->N)) != HC_OK) return rc;
+  double* drho = h->scratch;
+  double* du = h->scratch + h->N;
+  if (h->f64) HC_CUDA(h, hcd::launch_moments<double>(lbm_view<double>(h, h->cur, 1 - h->cur), drho, du, h->stream));
+  else HC_CUDA(h, hcd::launch_moments<float>(lbm_view<float>(h, h->cur, 1 - h->cur), drho, du, h->stream));
+  if (rho) HC_CUDA(h, cudaMemcpyAsync(rho, drho, 8 * h->N, cudaMemcpyDeviceToHost, h->stream));
+  if (u) HC_CUDA(h, cudaMemcpyAsync(u, du, 8 * 3 * h->N, cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_read_populations(hc_handle* h, double* f) {
+  if (!h || !f) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 19 * h->N)) != HC_OK) return rc;
+  if (h->f64) HC_CUDA(h, hcd::launch_convert_out<double>((const double*)h->f[h->cur], h->scratch, 19 * h->N, 1, h->N, h->stream));
+  else HC_CUDA(h, hcd::launch_convert_out<float>((const float*)h->f[h->cur], h->scratch, 19 * h->N, 1, h->N, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(f, h->scratch, 8 * 19 * h->N, cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_write_populations(hc_handle* h, const double* f) {
+  if (!h || !f) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 19 * h->N)) != HC_OK) return rc;
+  HC_CUDA(h, cudaMemcpyAsync(h->scratch, f, 8 * 19 * h->N, cudaMemcpyHostToDevice, h->stream));
+  if (h->f64) HC_CUDA(h, hcd::launch_convert_in<double>(h->scratch, (double*)h->f[h->cur], 19 * h->N, 1.0, h->N, h->stream));
+  else HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)h->f[h->cur], 19 * h->N, 1.0, h->N, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_read_force_field(hc_handle* h, double* F, int which) {
+  if (!h || !F) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 3 * h->N)) != HC_OK) return rc;
+  const void* src = h->F[which ? 1 - h->cur : h->cur];
+  if (h->f64) HC_CUDA(h, hcd::launch_convert_out<double>((const double*)src, h->scratch, 3 * h->N, 0, h->N, h->stream));
+  else HC_CUDA(h, hcd::launch_convert_out<float>((const float*)src, h->scratch, 3 * h->N, 0, h->N, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(F, h->scratch, 8 * 3 * h->N, cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_write_force_field(hc_handle* h, const double* F) {
+  if (!h || !F) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 3 * h->N)) != HC_OK) return rc;
+  HC_CUDA(h, cudaMemcpyAsync(h->scratch, F, 8 * 3 * h->N, cudaMemcpyHostToDevice, h->stream));
+  for (int k = 0; k < 2; ++k) {
+    if (h->f64) HC_CUDA(h, hcd::launch_convert_in<double>(h->scratch, (double*)h->F[k], 3 * h->N, 0.0, h->N, h->stream));
+    else HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)h->F[k], 3 * h->N, 0.0, h->N, h->stream));
+  }
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_read_vertices(hc_handle* h, double* x, double* v, double* f) {
+  if (!h) return HC_ERR_INVALID;
+  if (h->nvert == 0) return HC_OK;
+  int rc;
+  if (x && (rc = read3<double>(h, h->x, x)) != HC_OK) return rc;
+  if (h->f64) {
+    if (v && (rc = read3<double>(h, h->v, v)) != HC_OK) return rc;
+    if (f && (rc = read3<double>(h, h->fv, f)) != HC_OK) return rc;
+  } else {
+    if (v && (rc = read3<float>(h, h->v, v)) != HC_OK) return rc;
+    if (f && (rc = read3<float>(h, h->fv, f)) != HC_OK) return rc;
+  }
+  return HC_OK;
+}
+
+int hc_write_vertices(hc_handle* h, const double* x, const double* v, const double* f) {
+  if (!h) return HC_ERR_INVALID;
+  if (h->nvert == 0) return HC_OK;
+  int rc;
+  if (x && (rc = write3(h, h->x, 8, x)) != HC_OK) return rc;
+  if (v && (rc = write3(h, h->v, h->ts, v)) != HC_OK) return rc;
+  if (f && (rc = write3(h, h->fv, h->ts, f)) != HC_OK) return rc;
+  return HC_OK;
+}
+
+int hc_read_cells(hc_handle* h, int* alive, double* volume) {
+  if (!h) return HC_ERR_INVALID;
+  if (h->ncells == 0) return HC_OK;
+  std::vector<int> al(h->ncells);
+  HC_CUDA(h, cudaMemcpyAsync(al.data(), h->alive, 4 * h->ncells, cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (alive) std::memcpy(alive, al.data(), 4 * h->ncells);
+  if (volume) {
+    std::vector<double> x(3 * (size_t)h->nvert);
+    int rc = hc_read_vertices(h, x.data(), nullptr, nullptr);
+    if (rc != HC_OK) return rc;
+    for (int c = 0; c < h->ncells; ++c) {
+      const hcg::TypeConstants& tc = h->types[h->h_cell_type[c]].tc;
+      const double* X = x.data() + 3 * (size_t)h->h_cell_voff[c];
+      double vol = 0;
+      for (int k = 0; k < tc.nf; ++k) {
+        const double* v0 = X + 3 * tc.tris[3 * k];
+        const double* v1 = X + 3 * tc.tris[3 * k + 1];
+        const double* v2 = X + 3 * tc.tris[3 * k + 2];
+        vol += (-v2[0] * v1[1] * v0[2] + v1[0] * v2[1] * v0[2] + v2[0] * v0[1] * v1[2] - v0[0] * v2[1] * v1[2] -
+                v1[0] * v0[1] * v2[2] + v0[0] * v1[1] * v2[2]);
+      }
+      volume[c] = vol / 6.0;
+    }
+  }
+  return HC_OK;
+}
+
+int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_offsets, int* tile_vertices,
+                 int* tile_cell_offsets, int* tile_cells, int max_tile_cells) {
+  if (!h) return HC_ERR_INVALID;
+  int rc = hc_stage(h, HC_STAGE_BIN);
+  if (rc != HC_OK) return rc;
+  const int nt = h->ntiles;
+  std::vector<int> tco(nt + 1);
+  HC_CUDA(h, cudaMemcpyAsync(tco.data(), h->tile_cell_offsets, 4 * (nt + 1), cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (tco[nt] > max_tile_cells) return fail(h, HC_ERR_INVALID, "tile_cells buffer too small");
+  if (vertex_node && h->nvert)
+    HC_CUDA(h, cudaMemcpyAsync(vertex_node, h->vnode, 4 * h->nvert, cudaMemcpyDeviceToHost, h->stream));
+  if (vertex_tile && h->nvert)
+    HC_CUDA(h, cudaMemcpyAsync(vertex_tile, h->vtile, 4 * h->nvert, cudaMemcpyDeviceToHost, h->stream));
+  if (tile_offsets) HC_CUDA(h, cudaMemcpyAsync(tile_offsets, h->bin_offsets, 4 * (nt + 1), cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (tile_vertices && tile_offsets && tile_offsets[nt] > 0)
+    HC_CUDA(h, cudaMemcpyAsync(tile_vertices, h->tile_vertices, 4 * (size_t)tile_offsets[nt], cudaMemcpyDeviceToHost,
+                               h->stream));
+  if (tile_cell_offsets) std::memcpy(tile_cell_offsets, tco.data(), 4 * (nt + 1));
+  if (tile_cells && tco[nt] > 0)
+    HC_CUDA(h, cudaMemcpyAsync(tile_cells, h->tile_cells, 4 * (size_t)tco[nt], cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return nt;
+}
+
+int hc_get_stats(hc_handle* h, hc_stats* out) {
+  if (!h || !out) return HC_ERR_INVALID;
+  out->nodes = h->N;
+  out->vertices = h->nvert;
+  out->cells = h->ncells;
+  out->types = (int)h->types.size();
+  out->iter = h->iter;
+  out->tau = h->u.tau;
+  out->omega = 1.0 / h->u.tau;
+  out->device_bytes = h->device_bytes;
+  int alive = 0;
+  if (h->ncells) {
+    std::vector<int> al(h->ncells);
+    HC_CUDA(h, cudaMemcpyAsync(al.data(), h->alive, 4 * h->ncells, cudaMemcpyDeviceToHost, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int a : al) alive += a != 0;
+  }
+  out->cells_alive = alive;
+  return HC_OK;
+}
+
+int hc_device_status(hc_handle* h, unsigned int* status) {
+  if (!h || !status) return HC_ERR_INVALID;
+  HC_CUDA(h, cudaMemcpyAsync(status, h->status, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return HC_OK;
+}
+
+int hc_autotune(hc_handle* h, const char* cache_path) {
+  if (!h) return HC_ERR_INVALID;
+  return h->f64 ? autotune<double>(h, cache_path) : autotune<float>(h, cache_path);
+}
+
+int hc_get_tuning(hc_handle* h, int* out8) {
+  if (!h || !out8) return HC_ERR_INVALID;
+  std::memcpy(out8, h->tune, sizeof(h->tune));
+  return HC_OK;
+}
+
+int hc_set_tuning(hc_handle* h, const int* in8) {
+  if (!h || !in8) return HC_ERR_INVALID;
+  if (in8[0] <= 0 || in8[1] <= 0 || in8[0] * in8[1] > 256 || in8[0] % 32 != 0)
+    return fail(h, HC_ERR_INVALID, "collide-stream block must be a multiple of 32 wide and at most 256 threads");
+  for (int k = 2; k <= 4; ++k)
+    if (in8[k] <= 0 || in8[k] > 512 || in8[k] % 32 != 0) return fail(h, HC_ERR_INVALID, "bad block size");
+  std::memcpy(h->tune, in8, sizeof(h->tune));
+  invalidate_graph(h);
+  return HC_OK;
+}
+
+// ---- mesh helpers ---------------------------------------------------------
+static int copy_mesh(const hcg::Mesh& m, double* xyz, int max_nv, int* tris, int max_nf, int* nv, int* nf) {
+  if (nv) *nv = (int)m.v.size();
+  if (nf) *nf = (int)m.t.size();
+  if ((int)m.v.size() > max_nv || (int)m.t.size() > max_nf) return HC_ERR_INVALID;
+  for (size_t i = 0; i < m.v.size(); ++i) {
+    xyz[3 * i] = m.v[i].x;
+    xyz[3 * i + 1] = m.v[i].y;
+    xyz[3 * i + 2] = m.v[i].z;
+  }
+  for (size_t k = 0; k < m.t.size(); ++k)
+    for (int c = 0; c < 3; ++c) tris[3 * k + c] = m.t[k][c];
+  return HC_OK;
+}
+
+int hc_mesh_icosphere(int min_triangles, double radius, double* xyz, int max_nv, int* tris, int max_nf, int* nv,
+                      int* nf) {
+  if (min_triangles < 8 || min_triangles > 400000 || !(radius > 0)) return HC_ERR_INVALID;
+  return copy_mesh(hcg::icosphere(min_triangles, radius), xyz, max_nv, tris, max_nf, nv, nf);
+}
+int hc_mesh_rbc(int min_triangles, double radius, double* xyz, int max_nv, int* tris, int max_nf, int* nv, int* nf) {
+  if (min_triangles < 8 || min_triangles > 400000 || !(radius > 0)) return HC_ERR_INVALID;
+  return copy_mesh(hcg::rbc_from_sphere(min_triangles, radius), xyz, max_nv, tris, max_nf, nv, nf);
+}
+int hc_mesh_ellipsoid(int min_triangles, double radius, double aspect, double* xyz, int max_nv, int* tris, int max_nf,
+                      int* nv, int* nf) {
+  if (min_triangles < 8 || min_triangles > 400000 || !(radius > 0) || !(aspect > 0)) return HC_ERR_INVALID;
+  return copy_mesh(hcg::ellipsoid_from_sphere(min_triangles, radius, aspect), xyz, max_nv, tris, max_nf, nv, nf);
+}
+int hc_mesh_antipodal_pairs(const double* xyz, int nv, int* pairs, int max_pairs) {
+  if (!xyz || nv <= 0) return HC_ERR_INVALID;
+  std::vector<hcg::Vec3> v(nv);
+  for (int i = 0; i < nv; ++i) v[i] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+  auto pr = hcg::antipodal_pairs(v);
+  if ((int)pr.size() > max_pairs) return HC_ERR_INVALID;
+  for (size_t k = 0; k < pr.size(); ++k) {
+    pairs[2 * k] = pr[k][0];
+    pairs[2 * k + 1] = pr[k][1];
+  }
+  return (int)pr.size();
+}
+
+int hc_place_cells(const double* txyz, int nv, int n, const double* centres, const double* angles, double* out) {
+  if (!txyz || nv <= 0 || n < 0 || (n > 0 && (!centres || !angles || !out))) return HC_ERR_INVALID;
+  std::vector<hcg::Vec3> rest(nv);
+  for (int i = 0; i < nv; ++i) rest[i] = {txyz[3 * i], txyz[3 * i + 1], txyz[3 * i + 2]};
+  std::vector<double> xyz;
+  xyz.reserve(3 * (size_t)n * nv);
+  for (int c = 0; c < n; ++c) hcg::place_cell(rest, centres + 3 * c, angles + 3 * c, xyz);
+  std::memcpy(out, xyz.data(), sizeof(double) * xyz.size());
+  return HC_OK;
+}
+
+int hc_pack_cells(int nx, int ny, int nz, const int* periodic, const uint8_t* solid, int ntypes,
+                  const double* const* type_xyz, const int* type_nv, const int* const* type_tris, const int* type_nf,
+                  const int* counts, double margin, unsigned long long seed, int max_attempts, double* centres,
+                  double* angles, int* types) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || !periodic || ntypes <= 0 || !type_xyz || !type_nv || !type_tris ||
+      !type_nf || !counts || !centres || !angles || !types)
+    return HC_ERR_INVALID;
+  std::vector<hcg::Mesh> shapes(ntypes);
+  for (int t = 0; t < ntypes; ++t) {
+    for (int i = 0; i < type_nv[t]; ++i)
+      shapes[t].v.push_back({type_xyz[t][3 * i], type_xyz[t][3 * i + 1], type_xyz[t][3 * i + 2]});
+    for (int k = 0; k < type_nf[t]; ++k)
+      shapes[t].t.push_back({type_tris[t][3 * k], type_tris[t][3 * k + 1], type_tris[t][3 * k + 2]});
+  }
+  return hcg::pack_cells(nx, ny, nz, periodic, solid, ntypes, shapes, counts, margin, seed, max_attempts, centres,
+                         angles, types);
+}
+
+}  // extern "C"

@@ -1,0 +1,117 @@
+// Device-side views shared by the kernels (hc_kernels.cu) and the C ABI
+// (hc_api.cu).  All arrays are structure-of-arrays in HBM:
+//   populations f[19][N] stored as f_i - w_i (T = double or float)
+//   force field F[3][N] (T), double-buffered: the force of the collision in
+//   flight and the next step's force (body force + spreading)
+//   vertex x[3][V] (always double), v[3][V] and force[3][V] (T)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hcd {
+
+constexpr uint32_t NB_SOLID = 1u << 23;  // node itself is a wall node
+constexpr int NB_CLASS_SHIFT = 24;        // wall class of the bounce-back neighbours
+constexpr uint32_t NB_CLASS_MIXED = 255;  // neighbours of differing wall class
+constexpr int MAX_WALL_CLASSES = 16;
+constexpr int MAX_TYPES = 8;
+
+template <typename T>
+struct LbmView {
+  int nx, ny, nz;
+  int per[3];
+  long long N;
+  const T* __restrict__ fsrc;
+  T* __restrict__ fdst;
+  const T* __restrict__ Fcur;
+  T* __restrict__ Fnext;
+  const uint32_t* __restrict__ nbmask;
+  const uint8_t* __restrict__ flag;
+  const T* __restrict__ bodyz;  // [3][nz]
+  T omega;
+  T uw[MAX_WALL_CLASSES][3];
+};
+
+// Per-cell-type rest state and lattice-unit constants (device pointers).
+struct TypeDev {
+  int model, nv, nf, ne, ni;
+  const int* tris;        // nf*3
+  const int* edges;       // ne*2
+  const int* bend_tris;   // ne*2
+  const int* bend_outer;  // ne*2
+  const int* ring;        // nv*6
+  const int* ring_n;      // nv
+  const int* inner;       // ni*2
+  const double* tri_a0;
+  const double* edge_l0;
+  const double* edge_angle0;
+  const double* patch_d0;
+  const double* inner_l0;
+  double volume_eq, area_mean_eq, edge_mean_eq;
+  double k_link, k_bend, k_volume, k_area, eta_m, k_inner_rigid, k_cyto, core_radius, radius;
+};
+
+template <typename T>
+struct VertexView {
+  long long V;        // vertex capacity stride of the SoA arrays
+  int nvert;          // vertices in use
+  double* x;          // [3][V]
+  T* v;               // [3][V]
+  T* f;               // [3][V]
+  const int* vcell;   // vertex -> cell
+  int* alive;         // per cell
+  int* vnode;         // per vertex nearest node (or -1)
+  int* vtile;         // per vertex tile (or -1)
+  unsigned int* status;
+};
+
+struct TileGrid {
+  int tx, ty, tz;     // tile dims
+  int ntx, nty, ntz;  // tiles per axis
+};
+
+template <typename T>
+struct MechView {
+  const int* cells;   // cells to process
+  int ncells;
+  const int* cell_type;
+  const int* cell_voff;
+  const TypeDev* types;
+  VertexView<T> vv;
+  int dyn_smem;       // bytes available per CTA
+};
+
+// Launch wrappers (hc_kernels.cu); each enqueues on `s` and returns the
+// launch error code.
+template <typename T>
+cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s);
+template <typename T>
+cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs,
+                          cudaStream_t s);
+template <typename T>
+cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg,
+                                  int do_interp, int do_advance, int bs, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s);
+template <typename T>
+size_t mechanics_smem_bytes(int nv);
+template <typename T>
+cudaError_t prepare_mechanics(int smem_bytes);
+template <typename T>
+cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s);
+template <typename T>
+cudaError_t launch_convert_in(const double* src, T* dst, long long n, double shift_by_weight, long long N,
+                              cudaStream_t s);
+template <typename T>
+cudaError_t launch_convert_out(const T* src, double* dst, long long n, int add_weight, long long N,
+                               cudaStream_t s);
+template <typename T>
+cudaError_t launch_bin_vertices(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, cudaStream_t s);
+// binning: tile CSR sorted by (tile, cell, vertex)
+cudaError_t launch_bin_csr(const int* vtile, int nvert, int ntiles, int* counts, int* offsets, int* cursor,
+                           int* tile_vertices, const int* vcell, int* tile_cell_counts, cudaStream_t s);
+cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, const int* vcell, int ntiles,
+                              int* tile_cell_counts, int* tile_cell_offsets, int* tile_cells, int max_cells,
+                              cudaStream_t s);
+
+}  // namespace hcd

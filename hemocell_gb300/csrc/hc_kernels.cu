@@ -1,0 +1,951 @@
+// CUDA kernels of the GB300 HemoCell IB-LBM step (sm_103a).
+//
+//  K1 collide_stream   D3Q19 Guo-forced BGK, push streaming with (moving)
+//                      bounce-back and periodic wrap; writes the next step's
+//                      force field (body force) so the reset is fused.
+//  K2 spread           IBM phi2 force spreading (FP atomics into F).
+//  K3+K5 interp_advance IBM velocity interpolation from the post-stream
+//                      populations, Euler advance, nearest-node binning and
+//                      wall deletion, one thread per vertex.
+//  K4 mechanics        RBC / PLT / WBC membrane forces, one CTA per cell,
+//                      vertex forces accumulated in shared memory.
+//  bin_csr             per-tile vertex lists sorted by (tile, cell, vertex).
+//
+// Templated on T = double (plain form) or float (mixed form).  Positions are
+// double in both forms.
+#include <cmath>
+#include <cstdint>
+
+#include "hc_dev.h"
+
+namespace hcd {
+
+// ---------------------------------------------------------------------------
+// D3Q19 velocity set: 0 rest, 1..9 one half, i+9 the opposite of i.
+__host__ __device__ constexpr int cxi(int i) {
+  return (i == 1 || i == 4 || i == 5 || i == 6 || i == 7) ? -1
+         : (i == 10 || i == 13 || i == 14 || i == 15 || i == 16) ? 1 : 0;
+}
+__host__ __device__ constexpr int cyi(int i) {
+  return (i == 2 || i == 4 || i == 8 || i == 9 || i == 14) ? -1
+         : (i == 5 || i == 11 || i == 13 || i == 17 || i == 18) ? 1 : 0;
+}
+__host__ __device__ constexpr int czi(int i) {
+  return (i == 3 || i == 6 || i == 8 || i == 16 || i == 18) ? -1
+         : (i == 7 || i == 9 || i == 12 || i == 15 || i == 17) ? 1 : 0;
+}
+__host__ __device__ constexpr int oppi(int i) { return i == 0 ? 0 : (i <= 9 ? i + 9 : i - 9); }
+__host__ __device__ constexpr double wi(int i) {
+  return i == 0 ? 1.0 / 3.0 : ((cxi(i) * cxi(i) + cyi(i) * cyi(i) + czi(i) * czi(i)) == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
+}
+
+template <typename T>
+__device__ __forceinline__ T tmax(T a, T b) {
+  return a > b ? a : b;
+}
+
+// c . a for a lattice velocity c; the components are compile-time constants
+// once the direction loop is unrolled, so zero components cost nothing.
+template <typename T>
+__device__ __forceinline__ T cdot(int cx, int cy, int cz, T x, T y, T z) {
+  T r;
+  if (cx != 0) {
+    r = cx > 0 ? x : -x;
+    if (cy != 0) r = cy > 0 ? r + y : r - y;
+    if (cz != 0) r = cz > 0 ? r + z : r - z;
+  } else if (cy != 0) {
+    r = cy > 0 ? y : -y;
+    if (cz != 0) r = cz > 0 ? r + z : r - z;
+  } else {
+    r = cz > 0 ? z : (cz < 0 ? -z : T(0));
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// K1: collide + stream.  One thread per node; blocks are (bx, by) over x,y
+// and one z-plane per blockIdx.z.  The collision is written per opposite
+// pair (i, i+9) so the even and odd parts of equilibrium and Guo source are
+// shared: f*_{+c} = (1-w) f_{+c} + P + Q, f*_{-c} = (1-w) f_{-c} + P - Q.
+template <typename T>
+__global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (X >= L.nx || Y >= L.ny) return;
+  const long long N = L.N;
+  const long long n = (long long)X + (long long)L.nx * ((long long)Y + (long long)L.ny * Z);
+  const uint32_t m = __ldg(L.nbmask + n);
+  if (m & NB_SOLID) return;
+
+  T f[19];
+#pragma unroll
+  for (int i = 0; i < 19; ++i) f[i] = L.fsrc[i * N + n];
+  const T Fx = L.Fcur[n], Fy = L.Fcur[N + n], Fz = L.Fcur[2 * N + n];
+
+  T d[10], p[10];
+#pragma unroll
+  for (int i = 1; i <= 9; ++i) {
+    d[i] = f[i + 9] - f[i];
+    p[i] = f[i + 9] + f[i];
+  }
+  const T rhoBar = f[0] + ((p[1] + p[2]) + (p[3] + p[4])) + ((p[5] + p[6]) + (p[7] + p[8])) + p[9];
+  const T jx = (d[1] + d[4]) + (d[5] + d[6]) + d[7];
+  const T jy = (d[2] + d[4]) - d[5] + (d[8] + d[9]);
+  const T jz = (d[3] + d[6]) - d[7] + (d[8] - d[9]);
+  const T rho = T(1) + rhoBar;
+  const T invRho = T(1) / rho;
+  const T ux = (jx + T(0.5) * Fx) * invRho;
+  const T uy = (jy + T(0.5) * Fy) * invRho;
+  const T uz = (jz + T(0.5) * Fz) * invRho;
+  const T uu = ux * ux + uy * uy + uz * uz;
+  const T uF = ux * Fx + uy * Fy + uz * Fz;
+  const T om = L.omega;
+  const T om1 = T(1) - om;
+  const T hs = T(1) - T(0.5) * om;
+  const T A = rhoBar - T(1.5) * rho * uu;  // even equilibrium part, without w
+  const T B = T(4.5) * rho;
+  const T K = T(3) * rho * om;
+  const T G = T(-3) * hs * uF;
+  const T H = T(9) * hs;
+  const T Lc = T(3) * hs;
+  // weight classes: axis w=1/18 and diagonal w=1/36
+  const T w1 = T(1.0 / 18.0);
+  const T Aw1 = om * w1 * A, Bw1 = om * w1 * B, Gw1 = w1 * G, Hw1 = w1 * H, Kw1 = w1 * K, Lw1 = w1 * Lc;
+  const T Aw2 = T(0.5) * Aw1, Bw2 = T(0.5) * Bw1, Gw2 = T(0.5) * Gw1, Hw2 = T(0.5) * Hw1, Kw2 = T(0.5) * Kw1,
+          Lw2 = T(0.5) * Lw1;
+
+  T post[19];
+  post[0] = om1 * f[0] + T(1.0 / 3.0) * (om * A + G);
+#pragma unroll
+  for (int i = 1; i <= 9; ++i) {
+    const int j = i + 9;  // positive direction c = c_j
+    const T cu = cdot(cxi(j), cyi(j), czi(j), ux, uy, uz);
+    const T cF = cdot(cxi(j), cyi(j), czi(j), Fx, Fy, Fz);
+    const bool axis = (wi(j) > 1.0 / 20.0);
+    const T Aw = axis ? Aw1 : Aw2, Bw = axis ? Bw1 : Bw2, Gw = axis ? Gw1 : Gw2;
+    const T Hw = axis ? Hw1 : Hw2, Kw = axis ? Kw1 : Kw2, Lw = axis ? Lw1 : Lw2;
+    const T P = (Bw * (cu * cu) + Aw) + (Hw * (cu * cF) + Gw);
+    const T Q = Kw * cu + Lw * cF;
+    post[j] = om1 * f[j] + (P + Q);
+    post[i] = om1 * f[i] + (P - Q);
+  }
+
+  // streaming (push) with bounce-back
+  const int xm = X == 0 ? L.nx - 1 : X - 1, xp = X == L.nx - 1 ? 0 : X + 1;
+  const int ym = Y == 0 ? L.ny - 1 : Y - 1, yp = Y == L.ny - 1 ? 0 : Y + 1;
+  const int zm = Z == 0 ? L.nz - 1 : Z - 1, zp = Z == L.nz - 1 ? 0 : Z + 1;
+  const uint32_t cls = m >> NB_CLASS_SHIFT;
+  L.fdst[n] = post[0];
+#pragma unroll
+  for (int i = 1; i < 19; ++i) {
+    const int ox = cxi(i) < 0 ? xm : (cxi(i) > 0 ? xp : X);
+    const int oy = cyi(i) < 0 ? ym : (cyi(i) > 0 ? yp : Y);
+    const int oz = czi(i) < 0 ? zm : (czi(i) > 0 ? zp : Z);
+    if (m & (1u << (i - 1))) {
+      uint32_t c = cls;
+      if (c == NB_CLASS_MIXED) {
+        const bool out = (!L.per[0] && ((cxi(i) < 0 && X == 0) || (cxi(i) > 0 && X == L.nx - 1))) ||
+                         (!L.per[1] && ((cyi(i) < 0 && Y == 0) || (cyi(i) > 0 && Y == L.ny - 1))) ||
+                         (!L.per[2] && ((czi(i) < 0 && Z == 0) || (czi(i) > 0 && Z == L.nz - 1)));
+        c = out ? 0u : (uint32_t)L.flag[(long long)ox + (long long)L.nx * ((long long)oy + (long long)L.ny * oz)];
+        if (c >= (uint32_t)MAX_WALL_CLASSES) c = 0;
+      }
+      const T cuw = T(cxi(i)) * L.uw[c][0] + T(cyi(i)) * L.uw[c][1] + T(czi(i)) * L.uw[c][2];
+      L.fdst[oppi(i) * N + n] = post[i] - T(6.0 * wi(i)) * cuw;
+    } else {
+      const long long o = (long long)ox + (long long)L.nx * ((long long)oy + (long long)L.ny * oz);
+      L.fdst[i * N + o] = post[i];
+    }
+  }
+  L.Fnext[n] = L.bodyz[Z];
+  L.Fnext[N + n] = L.bodyz[L.nz + Z];
+  L.Fnext[2 * N + n] = L.bodyz[2 * L.nz + Z];
+}
+
+template <typename T>
+cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s) {
+  if (bx <= 0) bx = 64;
+  if (by <= 0) by = 4;
+  dim3 block(bx, by, 1);
+  dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
+  k_collide_stream<T><<<grid, block, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Node velocity of the post-stream populations with the collision force:
+// u = (sum_i c_i f_i + F/2) / rho   (Palabos computeVelocity for Guo forcing,
+// core/hemoCellParticleField.cpp:833).
+template <typename T>
+__device__ __forceinline__ void node_velocity(const T* __restrict__ f, const T* __restrict__ F, long long N,
+                                              long long n, T& ux, T& uy, T& uz) {
+  T d[10], p[10];
+  const T f0 = f[n];
+#pragma unroll
+  for (int i = 1; i <= 9; ++i) {
+    const T a = f[i * N + n], b = f[(i + 9) * N + n];
+    d[i] = b - a;
+    p[i] = b + a;
+  }
+  const T rhoBar = f0 + ((p[1] + p[2]) + (p[3] + p[4])) + ((p[5] + p[6]) + (p[7] + p[8])) + p[9];
+  const T jx = (d[1] + d[4]) + (d[5] + d[6]) + d[7];
+  const T jy = (d[2] + d[4]) - d[5] + (d[8] + d[9]);
+  const T jz = (d[3] + d[6]) - d[7] + (d[8] - d[9]);
+  const T rho = T(1) + rhoBar;
+  ux = (jx + T(0.5) * F[n]) / rho;
+  uy = (jy + T(0.5) * F[N + n]) / rho;
+  uz = (jz + T(0.5) * F[2 * N + n]) / rho;
+}
+
+// IBM phi2 kernel (core/immersedBoundaryMethod.h:37-41, :62-138).  The
+// reference scans the 3x3x3 nodes around floor(p+0.5) and keeps the nonzero
+// weights; phi2 vanishes beyond distance 1, so the kept nodes always lie in
+// the 2x2x2 block {floor(p), floor(p)+1}^3, which is scanned here in the same
+// (x, y, z) order.  Nodes off a non-periodic axis, zero weights and boundary
+// nodes are skipped (slot node = -1); the weights are renormalised to one.
+template <typename T>
+struct Kern {
+  long long node[8];
+  T w[8];
+};
+
+template <typename T>
+__device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, double py, double pz, Kern<T>& K) {
+  const double P[3] = {px, py, pz};
+  const int dims[3] = {L.nx, L.ny, L.nz};
+  T phi[3][2];
+  int idx[3][2];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const double q0 = floor(P[a]);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const double q = q0 + k;
+      const double r = P[a] - q;
+      phi[a][k] = tmax(T(1) - T(fabs(r)), T(0));
+      long long qi = (long long)q;
+      int wrapped;
+      if (qi < 0 || qi >= dims[a]) {
+        if (L.per[a]) {
+          long long mm = qi % dims[a];
+          wrapped = (int)(mm < 0 ? mm + dims[a] : mm);
+        } else {
+          wrapped = -1;
+        }
+      } else {
+        wrapped = (int)qi;
+      }
+      idx[a][k] = wrapped;
+    }
+  }
+  T total = T(0);
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int ax = s >> 2, ay = (s >> 1) & 1, az = s & 1;
+    K.node[s] = -1;
+    K.w[s] = T(0);
+    if (idx[0][ax] < 0 || idx[1][ay] < 0 || idx[2][az] < 0) continue;
+    const T w = phi[0][ax] * phi[1][ay] * phi[2][az];
+    if (w == T(0)) continue;
+    const long long nd =
+        (long long)idx[0][ax] + (long long)L.nx * ((long long)idx[1][ay] + (long long)L.ny * idx[2][az]);
+    if (L.flag[nd] != 0) continue;
+    total += w;
+    K.node[s] = nd;
+    K.w[s] = w;
+  }
+  if (total > T(0)) {
+    const T coeff = T(1) / total;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) K.w[s] *= coeff;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K2: spreadParticleForce (core/hemoCellParticleField.cpp:841-863) with the
+// FORCE_LIMIT clamp written back (:847-852).
+template <typename T>
+__global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const VertexView<T> vv, const T f_limit) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= vv.nvert) return;
+  if (!vv.alive[vv.vcell[i]]) return;
+  const long long V = vv.V;
+  T fx = vv.f[i], fy = vv.f[V + i], fz = vv.f[2 * V + i];
+  T mag = fx * fx;
+  mag += fy * fy;
+  mag += fz * fz;
+  mag = sqrt(mag);
+  if (mag > f_limit) {
+    const T s = f_limit / mag;
+    fx *= s;
+    fy *= s;
+    fz *= s;
+    vv.f[i] = fx;
+    vv.f[V + i] = fy;
+    vv.f[2 * V + i] = fz;
+  }
+  Kern<T> K;
+  ibm_weights(L, vv.x[i], vv.x[V + i], vv.x[2 * V + i], K);
+  T* F = const_cast<T*>(L.Fcur);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (K.node[j] < 0) continue;
+    atomicAdd(F + K.node[j], fx * K.w[j]);
+    atomicAdd(F + L.N + K.node[j], fy * K.w[j]);
+    atomicAdd(F + 2 * L.N + K.node[j], fz * K.w[j]);
+  }
+}
+
+template <typename T>
+cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs, cudaStream_t s) {
+  if (vv.nvert <= 0) return cudaSuccess;
+  if (bs <= 0) bs = 128;
+  k_spread<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, (T)f_limit);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// K3+K5: interpolateFluidVelocity (core/hemoCellParticleField.cpp:819-839),
+// advanceParticles (:566-588, core/hemoCellParticle.h:188-203) and the
+// per-vertex bin of update_pg (:137-168).  L.fsrc holds the post-stream
+// populations, L.Fcur the force of the collision that produced them.
+template <typename T>
+__global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, const VertexView<T> vv, const TileGrid tg,
+                                                        const int do_interp, const int do_advance) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= vv.nvert) return;
+  const int cell = vv.vcell[i];
+  if (!vv.alive[cell]) {
+    vv.vnode[i] = -1;
+    vv.vtile[i] = -1;
+    return;
+  }
+  const long long V = vv.V;
+  double px = vv.x[i], py = vv.x[V + i], pz = vv.x[2 * V + i];
+  T vx, vy, vz;
+  if (do_interp) {
+    Kern<T> K;
+    ibm_weights(L, px, py, pz, K);
+    vx = T(0);
+    vy = T(0);
+    vz = T(0);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (K.node[j] < 0) continue;
+      T ux, uy, uz;
+      node_velocity(L.fsrc, L.Fcur, L.N, K.node[j], ux, uy, uz);
+      vx += ux * K.w[j];
+      vy += uy * K.w[j];
+      vz += uz * K.w[j];
+    }
+    vv.v[i] = vx;
+    vv.v[V + i] = vy;
+    vv.v[2 * V + i] = vz;
+    if (!(isfinite((double)vx) && isfinite((double)vy) && isfinite((double)vz))) atomicOr(vv.status, 1u);
+  } else {
+    vx = vv.v[i];
+    vy = vv.v[V + i];
+    vz = vv.v[2 * V + i];
+  }
+  if (do_advance) {
+    px += (double)vx;
+    py += (double)vy;
+    pz += (double)vz;
+    vv.x[i] = px;
+    vv.x[V + i] = py;
+    vv.x[2 * V + i] = pz;
+  }
+  // nearest node and tile
+  const double P[3] = {px, py, pz};
+  const int dims[3] = {L.nx, L.ny, L.nz};
+  int q[3];
+  bool inside = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    long long qi = (long long)floor(P[a] + 0.5);
+    if (qi < 0 || qi >= dims[a]) {
+      if (L.per[a]) {
+        long long mm = qi % dims[a];
+        qi = mm < 0 ? mm + dims[a] : mm;
+      } else {
+        inside = false;
+      }
+    }
+    q[a] = (int)qi;
+  }
+  if (!inside) {
+    vv.vnode[i] = -1;
+    vv.vtile[i] = -1;
+    return;
+  }
+  const long long nd = (long long)q[0] + (long long)L.nx * ((long long)q[1] + (long long)L.ny * q[2]);
+  vv.vnode[i] = (int)nd;
+  vv.vtile[i] = q[0] / tg.tx + tg.ntx * (q[1] / tg.ty + tg.nty * (q[2] / tg.tz));
+  if (do_advance && L.flag[nd] != 0) {
+    vv.alive[cell] = 0;
+    atomicOr(vv.status, 2u);
+  }
+}
+
+template <typename T>
+cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, int do_interp,
+                                  int do_advance, int bs, cudaStream_t s) {
+  if (vv.nvert <= 0) return cudaSuccess;
+  if (bs <= 0) bs = 128;
+  k_interp_advance<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, tg, do_interp, do_advance);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// K4: constitutive models, one CTA per cell (grid-stride over the cell list).
+// Saturation constants: config/constant_defaults.h:157-173.
+constexpr double kMaxVol = 0.01, kMaxArea = 0.09, kMaxBend = 0.0555, kMaxPltBend = 2.467, kMaxLink = 9.0;
+constexpr double kForceLimit = 50.0;
+
+template <typename T>
+struct V3t {
+  T x, y, z;
+};
+template <typename T>
+__device__ __forceinline__ V3t<T> operator-(V3t<T> a, V3t<T> b) {
+  return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <typename T>
+__device__ __forceinline__ V3t<T> operator+(V3t<T> a, V3t<T> b) {
+  return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+template <typename T>
+__device__ __forceinline__ V3t<T> vscale(V3t<T> a, T s) {
+  return {a.x * s, a.y * s, a.z * s};
+}
+template <typename T>
+__device__ __forceinline__ V3t<T> vcross(V3t<T> a, V3t<T> b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <typename T>
+__device__ __forceinline__ T vdot(V3t<T> a, V3t<T> b) {
+  T r = a.x * b.x;
+  r += a.y * b.y;
+  r += a.z * b.z;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ T vnorm(V3t<T> a) {
+  return sqrt(vdot(a, a));
+}
+template <typename T>
+__device__ __forceinline__ V3t<T> ld3(const T* s, int k) {
+  return {s[3 * k], s[3 * k + 1], s[3 * k + 2]};
+}
+template <typename T>
+__device__ __forceinline__ void add3(T* s, int k, V3t<T> v) {
+  atomicAdd(s + 3 * k, v.x);
+  atomicAdd(s + 3 * k + 1, v.y);
+  atomicAdd(s + 3 * k + 2, v.z);
+}
+template <typename T>
+__device__ __forceinline__ V3t<T> unit_normal(V3t<T> a, V3t<T> b, V3t<T> c) {
+  V3t<T> n = vcross(b - a, c - a);
+  const T l = vnorm(n);
+  if (l != T(0)) return {n.x / l, n.y / l, n.z / l};
+  return {T(0), T(0), T(0)};
+}
+
+template <typename T>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    double s = lane < nw ? red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) red[32] = s;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+template <typename T>
+size_t mechanics_smem_bytes(int nv) {
+  return 34 * sizeof(double) + 6 * (size_t)nv * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
+  extern __shared__ double smem_d[];
+  double* red = smem_d;                  // 34 doubles
+  T* sx = reinterpret_cast<T*>(smem_d + 34);
+  const VertexView<T>& vv = M.vv;
+  const long long V = vv.V;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  constexpr bool kF64 = sizeof(T) == 8;
+  for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
+    const int cell = M.cells[ci];
+    const TypeDev& t = M.types[M.cell_type[cell]];
+    const int nv = t.nv;
+    const int voff = M.cell_voff[cell];
+    T* sf = sx + 3 * nv;
+    __syncthreads();  // previous cell fully written out
+    const bool alive = vv.alive[cell] != 0;
+    // positions: absolute in FP64, relative to vertex 0 in FP32
+    const double r0x = kF64 ? 0.0 : vv.x[voff], r0y = kF64 ? 0.0 : vv.x[V + voff],
+                 r0z = kF64 ? 0.0 : vv.x[2 * V + voff];
+    for (int k = tid; k < nv; k += bs) {
+      sx[3 * k] = (T)(vv.x[voff + k] - r0x);
+      sx[3 * k + 1] = (T)(vv.x[V + voff + k] - r0y);
+      sx[3 * k + 2] = (T)(vv.x[2 * V + voff + k] - r0z);
+      sf[3 * k] = T(0);
+      sf[3 * k + 1] = T(0);
+      sf[3 * k + 2] = T(0);
+    }
+    __syncthreads();
+    if (alive) {
+      // --- faces: volume, area force (rbcHighOrderModel.cpp:56-98)
+      double vol = 0.0;
+      for (int k = tid; k < t.nf; k += bs) {
+        const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
+        const V3t<T> v0 = ld3(sx, i0), v1 = ld3(sx, i1), v2 = ld3(sx, i2);
+        V3t<T> n = vcross(v1 - v0, v2 - v0);
+        if (kF64) {
+          const double v210 = (double)v2.x * v1.y * v0.z, v120 = (double)v1.x * v2.y * v0.z;
+          const double v201 = (double)v2.x * v0.y * v1.z, v021 = (double)v0.x * v2.y * v1.z;
+          const double v102 = (double)v1.x * v0.y * v2.z, v012 = (double)v0.x * v1.y * v2.z;
+          vol += (-v210 + v120 + v201 - v021 - v102 + v012);
+        } else {
+          // v0 . ((v1-v0) x (v2-v0)) == v0 . (v1 x v2); FP32 term, FP64 sum
+          vol += (double)vdot(v0, n);
+        }
+        const T nn = vnorm(n);
+        T area;
+        if (nn != T(0)) {
+          area = T(0.5) * nn;
+          n = {n.x / nn, n.y / nn, n.z / nn};
+        } else {
+          area = T(0);
+        }
+        const T a0 = (T)t.tri_a0[k];
+        const T ar = (area - a0) / a0;
+        const T afm = (T)t.k_area * (ar + ar / fabs(T(kMaxArea) - ar * ar));
+        const V3t<T> cen = {(v0.x + v1.x + v2.x) / T(3), (v0.y + v1.y + v2.y) / T(3), (v0.z + v1.z + v2.z) / T(3)};
+        add3(sf, i0, vscale(cen - v0, afm));
+        add3(sf, i1, vscale(cen - v1, afm));
+        add3(sf, i2, vscale(cen - v2, afm));
+      }
+      const double volume = block_sum<T>(vol, red) * (1.0 / 6.0);
+      const double vfr = (volume - t.volume_eq) / t.volume_eq;
+      const double vforce = -t.k_volume * vfr / fabs(kMaxVol - vfr * vfr);
+      // --- faces: volume force (:103-124)
+      for (int k = tid; k < t.nf; k += bs) {
+        const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
+        const V3t<T> v0 = ld3(sx, i0), v1 = ld3(sx, i1), v2 = ld3(sx, i2);
+        V3t<T> n = vcross(v1 - v0, v2 - v0);
+        const T nn = vnorm(n);
+        T area;
+        if (nn != T(0)) {
+          area = T(0.5) * nn;
+          n = {n.x / nn, n.y / nn, n.z / nn};
+        } else {
+          area = T(0);
+          n = {T(0), T(0), T(0)};
+        }
+        V3t<T> lvf;
+        if (kF64) {
+          lvf = vscale(vscale(n, (T)vforce), area / (T)t.area_mean_eq);
+        } else {
+          lvf = vscale(n, (T)(vforce * ((double)area / t.area_mean_eq)));
+        }
+        add3(sf, i0, lvf);
+        add3(sf, i1, lvf);
+        add3(sf, i2, lvf);
+      }
+      // --- vertices: bending (rbcHighOrderModel.cpp:127-166), RBC and WBC
+      if (t.model != 1) {
+        for (int i = tid; i < nv; i += bs) {
+          const int rn = t.ring_n[i];
+          const int* rg = t.ring + 6 * i;
+          const V3t<T> xi = ld3(sx, i);
+          V3t<T> sum = {T(0), T(0), T(0)};
+          for (int j = 0; j < rn; ++j) sum = sum + ld3(sx, rg[j]);
+          const V3t<T> mid = {sum.x / (T)rn, sum.y / (T)rn, sum.z / (T)rn};
+          const V3t<T> dev = mid - xi;
+          V3t<T> pn = {T(0), T(0), T(0)};
+          V3t<T> a = ld3(sx, rg[0]) - xi;
+          const V3t<T> first = a;
+          for (int j = 0; j < rn; ++j) {
+            const V3t<T> b = (j + 1 < rn) ? ld3(sx, rg[j + 1]) - xi : first;
+            V3t<T> tn = vcross(a, b);
+            const T l = vnorm(tn);
+            pn = pn + V3t<T>{tn.x / l, tn.y / l, tn.z / l};
+            a = b;
+          }
+          const T pl = vnorm(pn);
+          pn = {pn.x / pl, pn.y / pl, pn.z / pl};
+          const T ndev = vdot(pn, dev);
+          const T dDev = (ndev - (T)t.patch_d0[i]) / (T)t.edge_mean_eq;
+          const V3t<T> bf = vscale(pn, (T)t.k_bend * (dDev + dDev / fabs(T(kMaxBend) - dDev * dDev)));
+          add3(sf, i, bf);
+          const V3t<T> nbf = {-bf.x / (T)rn, -bf.y / (T)rn, -bf.z / (T)rn};
+          for (int j = 0; j < rn; ++j) add3(sf, rg[j], nbf);
+        }
+      }
+      // --- edges: link, membrane viscosity, platelet dihedral bending
+      const bool visc = (t.model != 0) || (t.eta_m != 0.0);
+      for (int e = tid; e < t.ne; e += bs) {
+        const int a = t.edges[2 * e], b = t.edges[2 * e + 1];
+        const V3t<T> p0 = ld3(sx, a), p1 = ld3(sx, b);
+        const V3t<T> ev = p1 - p0;
+        const T L = vnorm(ev);
+        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
+        const T l0 = (T)t.edge_l0[e];
+        const T ef = (L - l0) / l0;
+        const T fs = (T)t.k_link * (ef + ef / fabs(T(kMaxLink) - ef * ef));
+        const V3t<T> force = vscale(uv, fs);
+        V3t<T> fa = force, fb = {-force.x, -force.y, -force.z};
+        if (visc) {
+          const V3t<T> va = {vv.v[voff + a], vv.v[V + voff + a], vv.v[2 * V + voff + a]};
+          const V3t<T> vb = {vv.v[voff + b], vv.v[V + voff + b], vv.v[2 * V + voff + b]};
+          V3t<T> fv = vscale(vscale(uv, vdot(vb - va, uv)), (T)t.eta_m);
+          const T mm = vnorm(fv);
+          if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
+          fa = fa + fv;
+          fb = fb - fv;
+        }
+        if (t.model == 1) {
+          const int* A = t.tris + 3 * t.bend_tris[2 * e];
+          const int* B = t.tris + 3 * t.bend_tris[2 * e + 1];
+          const V3t<T> V1 = unit_normal(ld3(sx, A[0]), ld3(sx, A[1]), ld3(sx, A[2]));
+          const V3t<T> V2 = unit_normal(ld3(sx, B[0]), ld3(sx, B[1]), ld3(sx, B[2]));
+          const T angle = atan2(vdot(vcross(V1, V2), uv), vdot(V1, V2));
+          const T af = angle - (T)t.edge_angle0[e];
+          const T fm = (T)t.k_bend * (af + af / fabs(T(kMaxPltBend) - af * af));
+          const V3t<T> bfv = vscale(V1 + V2, fm * T(0.5));
+          fa = fa + bfv;
+          fb = fb + bfv;
+          const V3t<T> nb = {-bfv.x, -bfv.y, -bfv.z};
+          add3(sf, t.bend_outer[2 * e], nb);
+          add3(sf, t.bend_outer[2 * e + 1], nb);
+        }
+        add3(sf, a, fa);
+        add3(sf, b, fb);
+      }
+      // --- inner edges
+      for (int e = tid; e < t.ni; e += bs) {
+        const int a = t.inner[2 * e], b = t.inner[2 * e + 1];
+        const V3t<T> ev = ld3(sx, b) - ld3(sx, a);
+        const T L = vnorm(ev);
+        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
+        if (t.model == 1) {  // pltSimpleModel.cpp:188-205
+          const T l0 = (T)t.inner_l0[e];
+          const T ef = (L - l0) / l0;
+          const V3t<T> force = vscale(uv, (T)t.k_link * T(5) * ef);
+          add3(sf, a, force);
+          add3(sf, b, V3t<T>{-force.x, -force.y, -force.z});
+        } else if (t.model == 2) {  // wbcHighOrderModel.cpp:202-223
+          if (L < T(2) * (T)t.radius) {
+            const V3t<T> force = vscale(vscale(uv, T(1) - L / (T(2) * (T)t.radius)), (T)t.k_cyto);
+            add3(sf, a, V3t<T>{-force.x, -force.y, -force.z});
+            add3(sf, b, force);
+          }
+          if (L < T(2) * (T)t.core_radius) {
+            const V3t<T> force = vscale(vscale(uv, T(1) - L / (T(2) * (T)t.core_radius)), (T)t.k_inner_rigid);
+            add3(sf, a, V3t<T>{-force.x, -force.y, -force.z});
+            add3(sf, b, force);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < nv; k += bs) {
+      vv.f[voff + k] = sf[3 * k];
+      vv.f[V + voff + k] = sf[3 * k + 1];
+      vv.f[2 * V + voff + k] = sf[3 * k + 2];
+    }
+  }
+}
+
+// Raise the kernel's dynamic shared-memory limit (done when a cell type is
+// added, never inside a stream capture).
+template <typename T>
+cudaError_t prepare_mechanics(int smem_bytes) {
+  return cudaFuncSetAttribute(k_mechanics<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+}
+
+template <typename T>
+cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s) {
+  if (M.ncells <= 0) return cudaSuccess;
+  if (bs <= 0) bs = 256;
+  if (grid <= 0 || grid > M.ncells) grid = M.ncells;
+  k_mechanics<T><<<grid, bs, M.dyn_smem, s>>>(M);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Fluid readback: rho and u = (j + F/2)/rho of every node.
+template <typename T>
+__global__ void k_moments(const LbmView<T> L, double* rho, double* u) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L.N) return;
+  const long long N = L.N;
+  T rb = T(0);
+  for (int i = 0; i < 19; ++i) rb += L.fsrc[i * N + n];
+  T ux, uy, uz;
+  node_velocity(L.fsrc, L.Fcur, N, n, ux, uy, uz);
+  if (rho) rho[n] = 1.0 + (double)rb;
+  if (u) {
+    u[n] = ux;
+    u[N + n] = uy;
+    u[2 * N + n] = uz;
+  }
+}
+template <typename T>
+cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s) {
+  k_moments<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L, rho, u);
+  return cudaGetLastError();
+}
+
+// population / field conversion between double host layout and T device layout
+template <typename T>
+__global__ void k_convert_in(const double* src, T* dst, long long n, double shift, long long N) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s = 0.0;
+  if (shift != 0.0) {
+    const int i = (int)(k / N);
+    s = i == 0 ? 1.0 / 3.0 : (((i - 1) % 9) < 3 ? 1.0 / 18.0 : 1.0 / 36.0);
+  }
+  dst[k] = (T)(src[k] - s);
+}
+template <typename T>
+__global__ void k_convert_out(const T* src, double* dst, long long n, int add_w, long long N) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s = 0.0;
+  if (add_w) {
+    const int i = (int)(k / N);
+    s = i == 0 ? 1.0 / 3.0 : (((i - 1) % 9) < 3 ? 1.0 / 18.0 : 1.0 / 36.0);
+  }
+  dst[k] = (double)src[k] + s;
+}
+template <typename T>
+cudaError_t launch_convert_in(const double* src, T* dst, long long n, double shift, long long N, cudaStream_t s) {
+  k_convert_in<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n, shift, N);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_convert_out(const T* src, double* dst, long long n, int add_w, long long N, cudaStream_t s) {
+  k_convert_out<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n, add_w, N);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Per-vertex nearest node and tile from the current positions (update_pg,
+// core/hemoCellParticleField.cpp:137-168): bin = floor(x+0.5) wrapped on
+// periodic axes; vertices of removed cells or off a non-periodic axis get -1.
+template <typename T>
+__global__ void k_bin_vertices(const LbmView<T> L, const VertexView<T> vv, const TileGrid tg) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= vv.nvert) return;
+  const long long V = vv.V;
+  const double P[3] = {vv.x[i], vv.x[V + i], vv.x[2 * V + i]};
+  const int dims[3] = {L.nx, L.ny, L.nz};
+  int q[3];
+  bool inside = vv.alive[vv.vcell[i]] != 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    long long qi = (long long)floor(P[a] + 0.5);
+    if (qi < 0 || qi >= dims[a]) {
+      if (L.per[a]) {
+        long long mm = qi % dims[a];
+        qi = mm < 0 ? mm + dims[a] : mm;
+      } else {
+        inside = false;
+      }
+    }
+    q[a] = (int)qi;
+  }
+  if (!inside) {
+    vv.vnode[i] = -1;
+    vv.vtile[i] = -1;
+    return;
+  }
+  vv.vnode[i] = q[0] + L.nx * (q[1] + L.ny * q[2]);
+  vv.vtile[i] = q[0] / tg.tx + tg.ntx * (q[1] / tg.ty + tg.nty * (q[2] / tg.tz));
+}
+template <typename T>
+cudaError_t launch_bin_vertices(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, cudaStream_t s) {
+  if (vv.nvert <= 0) return cudaSuccess;
+  k_bin_vertices<T><<<(vv.nvert + 255) / 256, 256, 0, s>>>(L, vv, tg);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Binning CSR: counts per tile, exclusive scan, fill, per-tile sort by vertex
+// id (vertex ids grow with (cell, vertex id)), then per-tile unique cells.
+__global__ void k_bin_count(const int* vtile, int nvert, int* counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvert) return;
+  const int t = vtile[i];
+  if (t >= 0) atomicAdd(counts + t, 1);
+}
+
+// single-CTA exclusive scan of n ints into out[0..n]
+__global__ void k_scan(const int* in, int n, int* out) {
+  __shared__ int carry;
+  __shared__ int warp_sums[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    int v = i < n ? in[i] : 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      const int nw = blockDim.x >> 5;
+      int s = lane < nw ? warp_sums[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += y;
+      }
+      if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const int incl = x + (wid > 0 ? warp_sums[wid - 1] : 0);
+    if (i < n) out[i] = carry + incl - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void k_bin_fill(const int* vtile, int nvert, const int* offsets, int* cursor, int* tile_vertices) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvert) return;
+  const int t = vtile[i];
+  if (t < 0) return;
+  const int pos = offsets[t] + atomicAdd(cursor + t, 1);
+  tile_vertices[pos] = i;
+}
+
+// One CTA per tile: rank sort of the segment (keys are unique vertex ids),
+// then the number of distinct cells in the sorted segment.
+__global__ void k_bin_sort(const int* offsets, int* tile_vertices, const int* vcell, int* tile_cell_counts) {
+  __shared__ int buf[2048];
+  __shared__ int ncell;
+  const int t = blockIdx.x;
+  const int b = offsets[t], e = offsets[t + 1], len = e - b;
+  if (threadIdx.x == 0) ncell = 0;
+  if (len <= 0) {
+    if (threadIdx.x == 0) tile_cell_counts[t] = 0;
+    return;
+  }
+  if (len <= 2048) {
+    for (int k = threadIdx.x; k < len; k += blockDim.x) buf[k] = tile_vertices[b + k];
+    __syncthreads();
+    int out[8];
+    int cnt = 0;
+    for (int k = threadIdx.x; k < len; k += blockDim.x) {
+      const int key = buf[k];
+      int r = 0;
+      for (int j = 0; j < len; ++j) r += buf[j] < key;
+      out[cnt++] = r;
+    }
+    __syncthreads();
+    cnt = 0;
+    int keys[8];
+    for (int k = threadIdx.x; k < len; k += blockDim.x) keys[cnt++] = buf[k];
+    __syncthreads();
+    cnt = 0;
+    for (int k = threadIdx.x; k < len; k += blockDim.x) {
+      buf[out[cnt]] = keys[cnt];
+      cnt++;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < len; k += blockDim.x) tile_vertices[b + k] = buf[k];
+    int local = 0;
+    for (int k = threadIdx.x; k < len; k += blockDim.x)
+      local += (k == 0 || vcell[buf[k]] != vcell[buf[k - 1]]) ? 1 : 0;
+    atomicAdd(&ncell, local);
+    __syncthreads();
+    if (threadIdx.x == 0) tile_cell_counts[t] = ncell;
+  } else {
+    // large segment: serial insertion sort by one thread (rare)
+    if (threadIdx.x == 0) {
+      for (int k = b + 1; k < e; ++k) {
+        const int key = tile_vertices[k];
+        int j = k - 1;
+        while (j >= b && tile_vertices[j] > key) {
+          tile_vertices[j + 1] = tile_vertices[j];
+          --j;
+        }
+        tile_vertices[j + 1] = key;
+      }
+      int c = 0;
+      for (int k = b; k < e; ++k) c += (k == b || vcell[tile_vertices[k]] != vcell[tile_vertices[k - 1]]) ? 1 : 0;
+      tile_cell_counts[t] = c;
+    }
+  }
+}
+
+__global__ void k_tile_cells(const int* offsets, const int* tile_vertices, const int* vcell, int ntiles,
+                             const int* tile_cell_offsets, int* tile_cells, int max_cells) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  int o = tile_cell_offsets[t];
+  for (int k = offsets[t]; k < offsets[t + 1]; ++k) {
+    const int c = vcell[tile_vertices[k]];
+    if (k == offsets[t] || c != vcell[tile_vertices[k - 1]]) {
+      if (o < max_cells) tile_cells[o] = c;
+      o++;
+    }
+  }
+}
+
+cudaError_t launch_bin_csr(const int* vtile, int nvert, int ntiles, int* counts, int* offsets, int* cursor,
+                           int* tile_vertices, const int* vcell, int* tile_cell_counts, cudaStream_t s) {
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(counts, 0, sizeof(int) * ntiles, s)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(cursor, 0, sizeof(int) * ntiles, s)) != cudaSuccess) return e;
+  if (nvert > 0) k_bin_count<<<(nvert + 255) / 256, 256, 0, s>>>(vtile, nvert, counts);
+  k_scan<<<1, 1024, 0, s>>>(counts, ntiles, offsets);
+  if (nvert > 0) k_bin_fill<<<(nvert + 255) / 256, 256, 0, s>>>(vtile, nvert, offsets, cursor, tile_vertices);
+  k_bin_sort<<<ntiles, 256, 0, s>>>(offsets, tile_vertices, vcell, tile_cell_counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, const int* vcell, int ntiles,
+                              int* tile_cell_counts, int* tile_cell_offsets, int* tile_cells, int max_cells,
+                              cudaStream_t s) {
+  k_scan<<<1, 1024, 0, s>>>(tile_cell_counts, ntiles, tile_cell_offsets);
+  k_tile_cells<<<(ntiles + 255) / 256, 256, 0, s>>>(offsets, tile_vertices, vcell, ntiles, tile_cell_offsets,
+                                                    tile_cells, max_cells);
+  return cudaGetLastError();
+}
+
+// explicit instantiations
+#define HC_INST(T)                                                                                              \
+  template cudaError_t launch_collide_stream<T>(const LbmView<T>&, int, int, cudaStream_t);                    \
+  template cudaError_t launch_spread<T>(const LbmView<T>&, const VertexView<T>&, double, int, cudaStream_t);   \
+  template cudaError_t launch_interp_advance<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&, int, \
+                                                int, int, cudaStream_t);                                       \
+  template cudaError_t launch_mechanics<T>(const MechView<T>&, int, int, cudaStream_t);                        \
+  template size_t mechanics_smem_bytes<T>(int);                                                                \
+  template cudaError_t prepare_mechanics<T>(int);                                                              \
+  template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);                   \
+  template cudaError_t launch_bin_vertices<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&,         \
+                                              cudaStream_t);                                                   \
+  template cudaError_t launch_convert_in<T>(const double*, T*, long long, double, long long, cudaStream_t);     \
+  template cudaError_t launch_convert_out<T>(const T*, double*, long long, int, long long, cudaStream_t);
+HC_INST(double)
+HC_INST(float)
+
+}  // namespace hcd

@@ -1,0 +1,353 @@
+"""Python mirror of HemoCell's case-program API over the C ABI.
+
+Names follow the reference façade (hemocell.h:68-253): ``HemoCell``,
+``addCellType``, ``loadParticles``-style placement, ``iterate``,
+``setMaterialTimeScaleSeparation``, ``setParticleVelocityUpdateTimeScaleSeparation``
+and the driver's ``setExternalVector``.  Errors raise ``HemoCellError`` with
+the library's message (the reference prints through hlog and exits).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+
+class HemoCellError(RuntimeError):
+    pass
+
+
+def _dp(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(L.D)
+
+
+def _ip(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(L.I)
+
+
+@dataclass
+class Material:
+    """MaterialModel block of <celltype>.xml in SI units."""
+    kLink: float = 15.0
+    kBend: float = 80.0
+    kVolume: float = 20.0
+    kArea: float = 5.0
+    eta_m: float = 0.0
+    kInnerRigid: float = 0.0
+    kCytoskeleton: float = 0.0
+    coreRadius: float = 0.0
+    radius: float = 3.91e-6
+
+    def as_c(self) -> L.hc_material:
+        return L.hc_material(self.kLink, self.kBend, self.kVolume, self.kArea, self.eta_m, self.kInnerRigid,
+                             self.kCytoskeleton, self.coreRadius, self.radius)
+
+    def as_array(self) -> np.ndarray:
+        return np.array([self.kLink, self.kBend, self.kVolume, self.kArea, self.eta_m, self.kInnerRigid,
+                         self.kCytoskeleton, self.coreRadius, self.radius], dtype=np.float64)
+
+
+@dataclass
+class Mesh:
+    xyz: np.ndarray        # (nv, 3) float64, lattice units
+    tris: np.ndarray       # (nf, 3) int32, outward oriented
+    inner: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.int32))
+
+    @property
+    def nv(self) -> int:
+        return int(self.xyz.shape[0])
+
+    @property
+    def nf(self) -> int:
+        return int(self.tris.shape[0])
+
+
+def _mesh_call(fn, *args, est_nf: int) -> Mesh:
+    est_nv = est_nf // 2 + 2
+    xyz = np.zeros((est_nv, 3), np.float64)
+    tris = np.zeros((est_nf, 3), np.int32)
+    nv = C.c_int()
+    nf = C.c_int()
+    rc = fn(*args, _dp(xyz), est_nv, _ip(tris), est_nf, C.byref(nv), C.byref(nf))
+    if rc != L.HC_OK:
+        raise HemoCellError("mesh generation failed")
+    return Mesh(xyz[: nv.value].copy(), tris[: nf.value].copy())
+
+
+def _faces_for(min_triangles: int) -> int:
+    nf = 20
+    while nf < min_triangles:
+        nf *= 4
+    return nf
+
+
+def icosphere(min_triangles: int, radius: float) -> Mesh:
+    """WBC_SPHERE: constructSphereIcosahedron (helper/meshGeneratingFunctions.hh:31-151)."""
+    return _mesh_call(L.lib().hc_mesh_icosphere, min_triangles, radius, est_nf=_faces_for(min_triangles))
+
+
+def rbc_mesh(min_triangles: int, radius: float) -> Mesh:
+    """RBC_FROM_SPHERE: Evans-Fung biconcave map (helper/meshGeneratingFunctions.hh:153-168)."""
+    return _mesh_call(L.lib().hc_mesh_rbc, min_triangles, radius, est_nf=_faces_for(min_triangles))
+
+
+def ellipsoid_mesh(min_triangles: int, radius: float, aspect: float) -> Mesh:
+    """ELLIPSOID_FROM_SPHERE (helper/meshGeneratingFunctions.hh:170-183)."""
+    return _mesh_call(L.lib().hc_mesh_ellipsoid, min_triangles, radius, aspect, est_nf=_faces_for(min_triangles))
+
+
+def antipodal_pairs(xyz: np.ndarray) -> np.ndarray:
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    out = np.zeros((xyz.shape[0], 2), np.int32)
+    n = L.lib().hc_mesh_antipodal_pairs(_dp(xyz), xyz.shape[0], _ip(out), xyz.shape[0])
+    if n < 0:
+        raise HemoCellError("antipodal pair search failed")
+    return out[:n].copy()
+
+
+def place_cells(mesh: Mesh, centres: np.ndarray, angles: np.ndarray) -> np.ndarray:
+    """Vertex positions of cells placed as loadParticles does (io/readPositionsBloodCells.cpp:290-361)."""
+    centres = np.ascontiguousarray(centres, np.float64).reshape(-1, 3)
+    angles = np.ascontiguousarray(angles, np.float64).reshape(-1, 3)
+    n = centres.shape[0]
+    out = np.zeros((n * mesh.nv, 3), np.float64)
+    xyz = np.ascontiguousarray(mesh.xyz, np.float64)
+    rc = L.lib().hc_place_cells(_dp(xyz), mesh.nv, n, _dp(centres), _dp(angles), _dp(out))
+    if rc != L.HC_OK:
+        raise HemoCellError("placement failed")
+    return out
+
+
+def pack_cells(dims, periodic, solid: Optional[np.ndarray], meshes: Sequence[Mesh], counts: Sequence[int],
+               margin: float, seed: int, max_attempts: int = 20000):
+    """Seeded non-overlapping random packing; returns (centres, angles, types)."""
+    nt = len(meshes)
+    total = int(sum(counts))
+    xyzs = [np.ascontiguousarray(m.xyz, np.float64) for m in meshes]
+    triss = [np.ascontiguousarray(m.tris, np.int32) for m in meshes]
+    xp = (L.D * nt)(*[_dp(a) for a in xyzs])
+    tp = (L.I * nt)(*[_ip(a) for a in triss])
+    nvs = np.array([m.nv for m in meshes], np.int32)
+    nfs = np.array([m.nf for m in meshes], np.int32)
+    cnt = np.array(counts, np.int32)
+    per = np.array(periodic, np.int32)
+    centres = np.zeros((max(total, 1), 3), np.float64)
+    angles = np.zeros((max(total, 1), 3), np.float64)
+    types = np.zeros(max(total, 1), np.int32)
+    sp = None if solid is None else np.ascontiguousarray(solid, np.uint8).ctypes.data_as(L.U8)
+    n = L.lib().hc_pack_cells(dims[0], dims[1], dims[2], _ip(per), sp, nt, xp, _ip(nvs), tp, _ip(nfs), _ip(cnt),
+                              float(margin), C.c_ulonglong(seed), max_attempts, _dp(centres), _dp(angles), _ip(types))
+    if n < 0:
+        raise HemoCellError("packing failed")
+    return centres[:n].copy(), angles[:n].copy(), types[:n].copy()
+
+
+class HemoCell:
+    """One GB300-resident HemoCell instance (a D3Q19 lattice with its cells)."""
+
+    def __init__(self, nx: int, ny: int, nz: int, periodic=(1, 1, 1), dx: float = 0.5e-6, dt: float = 1e-7,
+                 nu_p: float = 0.0, rho_p: float = 1025.0, kBT_p: float = 4.100531391e-21, tau: float = 1.0,
+                 form: int = L.HC_FORM_PLAIN_F64, launch: int = L.HC_LAUNCH_PER_STAGE, device: int = 0,
+                 tile=(8, 8, 8)):
+        p = L.hc_params()
+        p.nx, p.ny, p.nz = nx, ny, nz
+        for a in range(3):
+            p.periodic[a] = int(periodic[a])
+            p.tile[a] = int(tile[a])
+        p.dx, p.dt, p.nu_p, p.rho_p, p.kBT_p, p.tau = dx, dt, nu_p, rho_p, kBT_p, tau
+        p.form, p.launch, p.device = form, launch, device
+        self._lib = L.lib()
+        h = self._lib.hc_create(C.byref(p))
+        if not h:
+            raise HemoCellError(self._lib.hc_last_error(None).decode())
+        self._h = C.c_void_p(h)
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.N = nx * ny * nz
+        self.form = form
+        self.types: list[Mesh] = []
+        self.cell_types: list[int] = []
+
+    # --- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.hc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            raise HemoCellError(self._lib.hc_last_error(self._h).decode() or f"error {rc}")
+        return rc
+
+    # --- units
+    def units(self) -> dict:
+        out = np.zeros(6)
+        self._check(self._lib.hc_derived_units(self._h, _dp(out)))
+        return dict(zip(("tau", "nu_lbm", "dm", "df", "kBT_lbm", "f_limit"), out.tolist()))
+
+    # --- lattice set-up
+    def set_flags(self, flags: np.ndarray):
+        f = np.ascontiguousarray(flags, np.uint8).reshape(-1)
+        assert f.size == self.N
+        self._check(self._lib.hc_set_flags(self._h, f.ctypes.data_as(L.U8)))
+
+    def set_wall_velocity(self, cls: int, u):
+        u = np.ascontiguousarray(u, np.float64)
+        self._check(self._lib.hc_set_wall_velocity(self._h, cls, _dp(u)))
+
+    def setExternalVector(self, mode: int, p=(0.0, 0.0, 0.0)):
+        p = np.ascontiguousarray(p, np.float64)
+        self._check(self._lib.hc_set_body_force(self._h, mode, _dp(p)))
+
+    set_body_force = setExternalVector
+
+    def latticeEquilibrium(self, rho: float = 1.0, u=(0.0, 0.0, 0.0)):
+        u = np.ascontiguousarray(u, np.float64)
+        self._check(self._lib.hc_init_equilibrium(self._h, rho, _dp(u)))
+
+    # --- cells
+    def addCellType(self, name: str, model: int, material: Material, mesh: Mesh) -> int:
+        xyz = np.ascontiguousarray(mesh.xyz, np.float64)
+        tris = np.ascontiguousarray(mesh.tris, np.int32)
+        inner = np.ascontiguousarray(mesh.inner, np.int32).reshape(-1, 2)
+        m = material.as_c()
+        t = self._check(self._lib.hc_add_cell_type(self._h, name.encode(), model, C.byref(m), _dp(xyz), mesh.nv,
+                                                   _ip(tris), mesh.nf, _ip(inner) if len(inner) else None,
+                                                   len(inner)))
+        self.types.append(mesh)
+        return t
+
+    def add_cells(self, type_id: int, centres: np.ndarray, angles: np.ndarray) -> int:
+        centres = np.ascontiguousarray(centres, np.float64).reshape(-1, 3)
+        angles = np.ascontiguousarray(angles, np.float64).reshape(-1, 3)
+        first = self._check(self._lib.hc_add_cells(self._h, type_id, centres.shape[0], _dp(centres), _dp(angles)))
+        self.cell_types += [type_id] * centres.shape[0]
+        return first
+
+    def add_cells_xyz(self, type_id: int, xyz: np.ndarray) -> int:
+        xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        n = xyz.shape[0] // self.types[type_id].nv
+        first = self._check(self._lib.hc_add_cells_xyz(self._h, type_id, n, _dp(xyz)))
+        self.cell_types += [type_id] * n
+        return first
+
+    def setMaterialTimeScaleSeparation(self, every: Sequence[int], velocity_every: int = 1):
+        e = np.ascontiguousarray(every, np.int32)
+        self._check(self._lib.hc_set_timescales(self._h, _ip(e), len(e), velocity_every))
+
+    # --- stepping
+    def iterate(self, nsteps: int = 1):
+        self._check(self._lib.hc_step(self._h, nsteps))
+
+    def stage(self, s: int):
+        self._check(self._lib.hc_stage(self._h, s))
+
+    def sync(self):
+        self._check(self._lib.hc_sync(self._h))
+
+    def time_steps(self, nsteps: int) -> float:
+        """Device time (ms) of nsteps, CUDA events on the handle's stream."""
+        ms = C.c_double()
+        self._check(self._lib.hc_time_steps(self._h, nsteps, C.byref(ms)))
+        return ms.value
+
+    def profile_stages(self, nsteps: int) -> dict:
+        out = np.zeros(5)
+        self._check(self._lib.hc_profile_stages(self._h, nsteps, _dp(out)))
+        return dict(zip(("spread", "collide_stream", "interp_advance", "mechanics", "step"), out.tolist()))
+
+    def read_positions(self, out: np.ndarray):
+        """Positions only, into a caller-owned (V,3) float64 buffer (pinned for speed)."""
+        self._check(self._lib.hc_read_vertices(self._h, _dp(out), None, None))
+        return out
+
+    # --- readback
+    def read_fluid(self):
+        rho = np.zeros(self.N)
+        u = np.zeros(3 * self.N)
+        self._check(self._lib.hc_read_fluid(self._h, _dp(rho), _dp(u)))
+        return rho, u.reshape(3, self.N)
+
+    def read_populations(self) -> np.ndarray:
+        f = np.zeros(19 * self.N)
+        self._check(self._lib.hc_read_populations(self._h, _dp(f)))
+        return f.reshape(19, self.N)
+
+    def write_populations(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, np.float64).reshape(-1)
+        self._check(self._lib.hc_write_populations(self._h, _dp(f)))
+
+    def read_force_field(self, which: int = 0) -> np.ndarray:
+        F = np.zeros(3 * self.N)
+        self._check(self._lib.hc_read_force_field(self._h, _dp(F), which))
+        return F.reshape(3, self.N)
+
+    def write_force_field(self, F: np.ndarray):
+        F = np.ascontiguousarray(F, np.float64).reshape(-1)
+        self._check(self._lib.hc_write_force_field(self._h, _dp(F)))
+
+    def stats(self) -> L.hc_stats:
+        s = L.hc_stats()
+        self._check(self._lib.hc_get_stats(self._h, C.byref(s)))
+        return s
+
+    def read_vertices(self):
+        V = self.stats().vertices
+        x = np.zeros((V, 3))
+        v = np.zeros((V, 3))
+        f = np.zeros((V, 3))
+        self._check(self._lib.hc_read_vertices(self._h, _dp(x), _dp(v), _dp(f)))
+        return x, v, f
+
+    def write_vertices(self, x=None, v=None, f=None):
+        conv = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (x, v, f)]
+        self._check(self._lib.hc_write_vertices(self._h, *[_dp(a) for a in conv]))
+
+    def read_cells(self):
+        n = self.stats().cells
+        alive = np.zeros(n, np.int32)
+        vol = np.zeros(n)
+        self._check(self._lib.hc_read_cells(self._h, _ip(alive), _dp(vol)))
+        return alive, vol
+
+    def read_bins(self):
+        st = self.stats()
+        V = st.vertices
+        # tiles are fixed by the parameters; size buffers generously
+        ntiles_max = self.N
+        vn = np.zeros(max(V, 1), np.int32)
+        vt = np.zeros(max(V, 1), np.int32)
+        to = np.zeros(ntiles_max + 1, np.int32)
+        tv = np.zeros(max(V, 1), np.int32)
+        tco = np.zeros(ntiles_max + 1, np.int32)
+        tc = np.zeros(max(V, 1), np.int32)
+        nt = self._check(self._lib.hc_read_bins(self._h, _ip(vn), _ip(vt), _ip(to), _ip(tv), _ip(tco), _ip(tc),
+                                                max(V, 1)))
+        return dict(vertex_node=vn[:V], vertex_tile=vt[:V], tile_offsets=to[: nt + 1],
+                    tile_vertices=tv[: to[nt]], tile_cell_offsets=tco[: nt + 1], tile_cells=tc[: tco[nt]])
+
+    def device_status(self) -> int:
+        s = C.c_uint()
+        self._check(self._lib.hc_device_status(self._h, C.byref(s)))
+        return s.value
+
+    def autotune(self, cache: str = ""):
+        self._check(self._lib.hc_autotune(self._h, cache.encode()))
+
+    def tuning(self) -> list:
+        t = np.zeros(8, np.int32)
+        self._check(self._lib.hc_get_tuning(self._h, _ip(t)))
+        return t.tolist()
+
+    def set_tuning(self, t):
+        t = np.ascontiguousarray(t, np.int32)
+        self._check(self._lib.hc_set_tuning(self._h, _ip(t)))

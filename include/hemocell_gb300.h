@@ -1,0 +1,191 @@
+/*
+ * hemocell_gb300 — C ABI of the GB300-native HemoCell IB-LBM time step.
+ *
+ * One handle (hc_handle) is one HemoCell instance: a D3Q19 lattice, its
+ * cell types and cells, all resident on one GPU.  Device memory is owned by
+ * the handle; host pointers passed in are borrowed for the call only.  No C++
+ * exception crosses this boundary: every call returns HC_OK (0) or a negative
+ * HC_ERR_* code, and hc_last_error(h) describes the last failure (like the
+ * reference's hlog message + exit(1), minus the exit).  A handle is
+ * thread-compatible: do not use one handle from two host threads at once.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the HemoCell source tree).
+ */
+#ifndef HEMOCELL_GB300_H
+#define HEMOCELL_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HC_OK 0
+#define HC_ERR_INVALID (-1)   /* bad argument (config/config.cpp:80-87 throws here) */
+#define HC_ERR_CUDA (-2)      /* CUDA runtime failure */
+#define HC_ERR_MEMORY (-3)    /* device memory exhausted / admission refused */
+#define HC_ERR_STATE (-4)     /* call not valid in the current state */
+#define HC_ERR_NUMERIC (-5)   /* NaN / non-finite state detected */
+
+/* precision forms */
+#define HC_FORM_PLAIN_F64 0   /* everything FP64 */
+#define HC_FORM_MIXED_F32 1   /* FP32 f_i - w_i populations, FP32 forces; FP64 positions,
+                                 per-cell volume sums and area/volume constraint terms */
+/* launch modes */
+#define HC_LAUNCH_PER_STAGE 0 /* one kernel per stage and per cell type */
+#define HC_LAUNCH_BATCHED 1   /* one launch per stage across cell types; step captured
+                                 as a CUDA graph */
+
+/* constitutive models (the Mechanics template argument of addCellType) */
+#define HC_MODEL_RBC_HIGH_ORDER 0 /* mechanics/rbcHighOrderModel.cpp */
+#define HC_MODEL_PLT_SIMPLE 1     /* mechanics/pltSimpleModel.cpp */
+#define HC_MODEL_WBC_HIGH_ORDER 2 /* mechanics/wbcHighOrderModel.cpp */
+
+/* body-force modes (the driver's setExternalVector after iterate()) */
+#define HC_BODY_NONE 0
+#define HC_BODY_UNIFORM 1     /* p[0..2] */
+#define HC_BODY_KOLMOGOROV 2  /* F_x = p[0] * sin(2 pi z / nz) */
+
+/* stages of HemoCell::iterate (core/hemoCell.cpp:299-376) */
+#define HC_STAGE_SPREAD 0         /* spreadParticleForce */
+#define HC_STAGE_COLLIDE_STREAM 1 /* lattice->collideAndStream + force reset */
+#define HC_STAGE_INTERPOLATE 2    /* interpolateFluidVelocity */
+#define HC_STAGE_ADVANCE 3        /* advanceParticles (+ binning of each vertex) */
+#define HC_STAGE_MECHANICS 4      /* applyConstitutiveModel (due types) */
+#define HC_STAGE_MECHANICS_FORCED 5 /* applyConstitutiveModel(forced=true) */
+#define HC_STAGE_BIN 6            /* tile CSR + per-tile cell lists */
+
+typedef struct hc_handle hc_handle;
+
+/* Simulation parameters: the <domain> block of config.xml plus the lattice
+ * the case program builds (examples/oneCellShear/oneCellShear.cpp:50-67). */
+typedef struct hc_params {
+  int nx, ny, nz;
+  int periodic[3];
+  double dx, dt;        /* [m], [s] */
+  double nu_p, rho_p;   /* [m^2/s], [kg/m^3] */
+  double kBT_p;         /* [J] */
+  double tau;           /* > 0: fixes tau; <= 0: tau = 3 nu_p dt / dx^2 + 1/2 */
+  int form;             /* HC_FORM_* */
+  int launch;           /* HC_LAUNCH_* */
+  int device;           /* CUDA device ordinal */
+  int tile[3];          /* binning tile (0 => 8) */
+} hc_params;
+
+/* MaterialModel block of <celltype>.xml, SI units
+ * (examples/oneCellShear/RBC.xml, examples/cell_shapes/WBC_HO.xml). */
+typedef struct hc_material {
+  double kLink, kBend, kVolume, kArea, eta_m;
+  double kInnerRigid, kCytoskeleton, coreRadius, radius;
+} hc_material;
+
+typedef struct hc_stats {
+  long long nodes;
+  int vertices, cells, cells_alive, types;
+  int iter;
+  double tau, omega;
+  long long device_bytes;
+} hc_stats;
+
+/* --- lifecycle: HemoCell::HemoCell / ~HemoCell (core/hemoCell.cpp:69-127) */
+hc_handle* hc_create(const hc_params* p);
+int hc_destroy(hc_handle* h);
+const char* hc_last_error(const hc_handle* h); /* h may be NULL: last create error */
+/* Parameters::lbm_base_parameters (mechanics/constantConversion.cpp:36-59):
+ * out = {tau, nu_lbm, dm, df, kBT_lbm, f_limit} */
+int hc_derived_units(const hc_handle* h, double* out6);
+
+/* --- lattice set-up (boundary flags helper/genericFunctions.cpp:138-159,
+ * shear walls helper/hemocellInit.hh:58-92, body force
+ * examples/pipeflow/pipeflow.cpp:141-146, lattice.initialize()) */
+int hc_set_flags(hc_handle* h, const uint8_t* flags); /* per node: 0 fluid, k>0 wall class k */
+int hc_set_wall_velocity(hc_handle* h, int cls, const double* u3);
+int hc_set_body_force(hc_handle* h, int mode, const double* p);
+int hc_init_equilibrium(hc_handle* h, double rho, const double* u3);
+
+/* --- cell types: HemoCell::addCellType<Mechanics>(name, shape)
+ * (hemocell.h:122-127; CommonCellConstants mechanics/commonCellConstants.cpp:70-409).
+ * template_xyz: nv*3 lattice-unit vertices of the rest shape; tris nf*3
+ * outward-oriented; inner nI*2 (InnerEdges).  Returns the type id (>= 0). */
+int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_material* m,
+                     const double* template_xyz, int nv, const int* tris, int nf,
+                     const int* inner_edges, int ni);
+/* HemoCell::loadParticles (io/readPositionsBloodCells.cpp:290-361): place n
+ * cells of a type, centred on their bounding box, rotated by
+ * rotateTriangularMeshXYZ(angles in rad) and translated to centres (lattice
+ * units).  Returns the first new cell id. */
+int hc_add_cells(hc_handle* h, int type, int n, const double* centres, const double* angles);
+/* place n cells from explicit vertex positions (n*nv*3, lattice units) */
+int hc_add_cells_xyz(hc_handle* h, int type, int n, const double* xyz);
+/* setMaterialTimeScaleSeparation / setParticleVelocityUpdateTimeScaleSeparation
+ * (hemocell.h:150,159; checked as in core/hemoCell.cpp:620-627) */
+int hc_set_timescales(hc_handle* h, const int* material_every, int ntypes, int velocity_every);
+
+/* --- the hot path: HemoCell::iterate() (core/hemoCell.cpp:299-376) */
+int hc_step(hc_handle* h, int nsteps);
+int hc_stage(hc_handle* h, int stage); /* one stage, for stage-wise parity */
+int hc_sync(hc_handle* h);
+
+/* timing with CUDA events recorded on the handle's stream (the stream every
+ * kernel of the step is launched on): hc_time_steps runs nsteps exactly as
+ * hc_step and returns the elapsed device time; hc_profile_stages runs nsteps
+ * with an event between stages (no graph) and returns the mean per step of
+ * {spread, collide_stream, interpolate+advance, mechanics, whole step} in ms */
+int hc_time_steps(hc_handle* h, int nsteps, double* ms);
+int hc_profile_stages(hc_handle* h, int nsteps, double* ms5);
+
+/* --- readback (io/FluidHdf5IO.hh velocity/density, io/ParticleHdf5IO.cpp) */
+int hc_read_fluid(hc_handle* h, double* rho, double* u);        /* rho[N], u[3][N] */
+int hc_read_populations(hc_handle* h, double* f);              /* f[19][N], unshifted */
+int hc_write_populations(hc_handle* h, const double* f);
+int hc_read_force_field(hc_handle* h, double* F, int which);   /* 0 next, 1 last collision */
+int hc_write_force_field(hc_handle* h, const double* F);       /* sets the next force field */
+int hc_read_vertices(hc_handle* h, double* x, double* v, double* f); /* [V][3] each, may be NULL */
+int hc_write_vertices(hc_handle* h, const double* x, const double* v, const double* f);
+int hc_read_cells(hc_handle* h, int* alive, double* volume);
+/* update_pg / ownership / neighbour lists (core/hemoCellParticleField.cpp:137-168):
+ * vertex_node[V], vertex_tile[V], tile_offsets[ntiles+1], tile_vertices[V],
+ * tile_cell_offsets[ntiles+1], tile_cells[max_tile_cells].  Returns ntiles. */
+int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_offsets,
+                 int* tile_vertices, int* tile_cell_offsets, int* tile_cells, int max_tile_cells);
+int hc_get_stats(hc_handle* h, hc_stats* out);
+/* last device status word: bit0 non-finite vertex velocity, bit1 cell deleted at a wall */
+int hc_device_status(hc_handle* h, unsigned int* status);
+
+/* --- launch tuning (project autotuner; results cached on disk) */
+int hc_autotune(hc_handle* h, const char* cache_path);
+int hc_get_tuning(hc_handle* h, int* out8);
+int hc_set_tuning(hc_handle* h, const int* in8);
+
+/* --- mesh helpers (helper/meshGeneratingFunctions.hh:31-271).  Buffers are
+ * caller-owned; sizes are checked against max_nv / max_nf. */
+/* icosphere refined until nf >= min_triangles (constructSphereIcosahedron) */
+int hc_mesh_icosphere(int min_triangles, double radius, double* xyz, int max_nv, int* tris,
+                      int max_nf, int* nv, int* nf);
+/* RBC_FROM_SPHERE: Evans-Fung biconcave map of the icosphere, radius in lattice units */
+int hc_mesh_rbc(int min_triangles, double radius, double* xyz, int max_nv, int* tris, int max_nf,
+                int* nv, int* nf);
+/* ELLIPSOID_FROM_SPHERE: x,y scaled by radius, z by aspect*radius */
+int hc_mesh_ellipsoid(int min_triangles, double radius, double aspect, double* xyz, int max_nv,
+                      int* tris, int max_nf, int* nv, int* nf);
+/* antipodal vertex pairs of a centrally symmetric mesh (inner edges) */
+int hc_mesh_antipodal_pairs(const double* xyz, int nv, int* pairs, int max_pairs);
+/* host-only placement used by hc_add_cells: n cells of one rest shape,
+ * centred on the bounding box, rotated (rotateTriangularMeshXYZ, angles in
+ * rad) and translated; out_xyz holds n*nv*3 doubles */
+int hc_place_cells(const double* template_xyz, int nv, int n, const double* centres, const double* angles,
+                   double* out_xyz);
+/* seeded non-overlapping packing of cells (see DESIGN: replaces tools/packCells):
+ * type_xyz/type_nv/type_tris/type_nf describe ntypes rest shapes, counts[t]
+ * cells per type; solid[N] marks forbidden nodes (may be NULL); margin in
+ * lattice units.  Writes centres[total*3], angles[total*3], types[total];
+ * returns the number of cells placed. */
+int hc_pack_cells(int nx, int ny, int nz, const int* periodic, const uint8_t* solid, int ntypes,
+                  const double* const* type_xyz, const int* type_nv, const int* const* type_tris,
+                  const int* type_nf, const int* counts, double margin, unsigned long long seed,
+                  int max_attempts, double* centres, double* angles, int* types);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,271 @@
+"""GPU parity of every stage of the IB-LBM step against the FP64 CPU oracle.
+
+All calls go through the C ABI (libhcgpu.so via ctypes).  Tolerances:
+  plain FP64 form: relative L2 <= 1e-12 for one stage, <= 1e-10 for runs of
+  hundreds of steps (FP atomics and FMA contraction reorder roundings);
+  integer outputs (bins, tile lists, cell ownership): bit-exact.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+STAGE_TOL = 1e-12
+RUN_TOL = 1e-10
+
+
+def _cases():
+    from hemocell_gb300 import cases
+    return cases
+
+
+def _orc():
+    from oracle import oracle
+    return oracle
+
+
+def mixed_box(seed=5, n=(20, 18, 16), wall=True):
+    """Small box with all three cell types and (optionally) moving walls."""
+    C = _cases()
+    nx, ny, nz = n
+    if wall:
+        flags, walls = C.shear_walls(n, 5000.0)
+        periodic = (1, 1, 0)
+    else:
+        flags, walls, periodic = None, {}, (1, 1, 1)
+    types = [C.rbc_type(320), C.plt_type(80, radius_m=1.0e-6, aspect=0.4), C.wbc_type(320)]
+    rng = np.random.default_rng(seed)
+    cells = []
+    centres = [((nx - 1) / 2, (ny - 1) / 2 - 3.5, (nz - 1) / 2), ((nx - 1) / 2 + 4, (ny - 1) / 2 + 5, (nz - 1) / 2),
+               ((nx - 1) / 2 - 4.5, (ny - 1) / 2 + 4.0, (nz - 1) / 2 + 1)]
+    for t, c in enumerate(centres):
+        ang = rng.uniform(-np.pi, np.pi, size=(1, 3))
+        xyz = C.place_cells(types[t].mesh, np.array([c]), ang)
+        cells.append((t, xyz))
+    case = C.Case("mixed_box", n, periodic, flags=flags, walls=walls, types=types, cells=cells,
+                  body_mode=1, body=(2e-6, -1e-6, 5e-7))
+    return case
+
+
+def randomize(case, hc, o, seed=11, amp=2e-3, famp=1e-4, xamp=0.05, vamp=1e-3):
+    """Identical random populations, force field and vertex perturbations on both."""
+    rng = np.random.default_rng(seed)
+    w = np.array([1 / 3] + [1 / 18] * 3 + [1 / 36] * 6 + [1 / 18] * 3 + [1 / 36] * 6)
+    f = w[:, None] * (1.0 + amp * rng.standard_normal((19, case.N)))
+    F = famp * rng.standard_normal((3, case.N))
+    hc.write_populations(f)
+    o.write_populations(f)
+    hc.write_force_field(F)
+    o.write_force_field(F)
+    x, _, _ = o.read_vertices()
+    x = x + xamp * rng.standard_normal(x.shape)
+    v = vamp * rng.standard_normal(x.shape)
+    fv = 1e-4 * rng.standard_normal(x.shape)
+    hc.write_vertices(x, v, fv)
+    o.write_vertices(x, v, fv)
+    return f, F, x, v, fv
+
+
+def test_collide_stream_one_stage(built):
+    case = mixed_box()
+    hc = case.build()
+    o = _orc().apply_case(case)
+    randomize(case, hc, o)
+    hc.stage(1)
+    o.stage("collide_stream")
+    fg, fo = hc.read_populations(), o.read_populations()
+    fluid = case.flags_array() == 0
+    assert rel_l2(fg[:, fluid], fo[:, fluid]) < STAGE_TOL
+    assert rel_l2(hc.read_force_field(0)[:, fluid], o.read_force_field(0)[:, fluid]) < STAGE_TOL
+    assert rel_l2(hc.read_force_field(1), o.read_force_field(1)) < STAGE_TOL
+    hc.close()
+
+
+def test_fluid_only_shear_100_steps(built):
+    C = _cases()
+    n = (16, 12, 20)
+    flags, walls = C.shear_walls(n, 20000.0)
+    case = C.Case("couette", n, (1, 1, 0), flags=flags, walls=walls, body_mode=1, body=(1e-6, 0, 0))
+    hc = case.build()
+    o = _orc().apply_case(case)
+    hc.iterate(100)
+    o.step(100)
+    rg, ug = hc.read_fluid()
+    ro, uo = o.read_fluid()
+    fluid = flags == 0
+    assert rel_l2(ug[:, fluid], uo[:, fluid]) < RUN_TOL
+    assert rel_l2(rg[fluid], ro[fluid]) < RUN_TOL
+    hc.close()
+
+
+def test_spread_stage(built):
+    case = mixed_box()
+    hc = case.build()
+    o = _orc().apply_case(case)
+    randomize(case, hc, o)
+    hc.stage(0)
+    o.stage("spread")
+    assert rel_l2(hc.read_force_field(0), o.read_force_field(0)) < STAGE_TOL
+    _, _, fg = hc.read_vertices()
+    _, _, fo = o.read_vertices()
+    assert rel_l2(fg, fo) < STAGE_TOL
+    hc.close()
+
+
+def test_spread_force_limit_clamp(built):
+    case = mixed_box()
+    hc = case.build()
+    o = _orc().apply_case(case)
+    randomize(case, hc, o)
+    x, _, _ = o.read_vertices()
+    big = np.zeros_like(x)
+    big[::7] = 0.05  # above f_limit (7.8e-3 lattice units)
+    hc.write_vertices(None, None, big)
+    o.write_vertices(None, None, big)
+    hc.stage(0)
+    o.stage("spread")
+    _, _, fg = hc.read_vertices()
+    _, _, fo = o.read_vertices()
+    assert np.max(np.linalg.norm(fg, axis=1)) <= hc.units()["f_limit"] * (1 + 1e-12)
+    assert rel_l2(fg, fo) < STAGE_TOL
+    assert rel_l2(hc.read_force_field(0), o.read_force_field(0)) < STAGE_TOL
+    hc.close()
+
+
+def test_interpolate_stage(built):
+    case = mixed_box()
+    hc = case.build()
+    o = _orc().apply_case(case)
+    randomize(case, hc, o)
+    hc.stage(2)
+    o.stage("interpolate")
+    _, vg, _ = hc.read_vertices()
+    _, vo, _ = o.read_vertices()
+    assert rel_l2(vg, vo) < STAGE_TOL
+    hc.close()
+
+
+def test_advance_and_bins_bit_exact(built):
+    case = mixed_box()
+    hc = case.build()
+    o = _orc().apply_case(case)
+    randomize(case, hc, o, vamp=0.3)
+    hc.stage(3)
+    o.stage("advance")
+    xg, _, _ = hc.read_vertices()
+    xo, _, _ = o.read_vertices()
+    assert np.array_equal(xg, xo)  # x + v in FP64, one rounding on both sides
+    ag, _ = hc.read_cells()
+    ao, _ = o.read_cells()
+    assert np.array_equal(ag, ao)
+    bg = hc.read_bins()
+    bo = o.bins((8, 8, 8), None, case.dims)
+    for k in bo:
+        assert np.array_equal(bg[k], bo[k]), k
+    hc.close()
+
+
+@pytest.mark.parametrize("types", [[0], [1], [2], [0, 1, 2]])
+def test_mechanics_stage(built, types):
+    case = mixed_box()
+    case.cells = [c for c in case.cells if c[0] in types]
+    hc = case.build()
+    o = _orc().apply_case(case)
+    randomize(case, hc, o, xamp=0.08)
+    hc.stage(5)
+    o.stage("mechanics", forced=1)
+    _, _, fg = hc.read_vertices()
+    _, _, fo = o.read_vertices()
+    assert np.abs(fo).max() > 0
+    assert rel_l2(fg, fo) < STAGE_TOL
+    hc.close()
+
+
+def test_full_step_shear_rbc(built):
+    C = _cases()
+    case = C.shear_single_rbc(n=24, shear_rate=20000.0, seed=7, min_triangles=320)
+    hc = case.build()
+    o = _orc().apply_case(case)
+    hc.iterate(300)
+    o.step(300)
+    xg, vg, fg = hc.read_vertices()
+    xo, vo, fo = o.read_vertices()
+    rg, ug = hc.read_fluid()
+    ro, uo = o.read_fluid()
+    assert rel_l2(xg, xo) < RUN_TOL
+    assert rel_l2(vg, vo) < RUN_TOL
+    assert rel_l2(fg, fo) < 1e-8
+    assert rel_l2(ug, uo) < RUN_TOL
+    assert rel_l2(rg, ro) < RUN_TOL
+    hc.close()
+
+
+def test_full_step_mixed_types_batched_graph(built):
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=False)
+    o = _orc().apply_case(case)
+    hp = case.build(launch=L.HC_LAUNCH_PER_STAGE)
+    hb = case.build(launch=L.HC_LAUNCH_BATCHED)
+    hp.iterate(100)
+    hb.iterate(100)  # graph replay (2 steps per launch)
+    o.step(100)
+    xo, vo, _ = o.read_vertices()
+    for hc in (hp, hb):
+        xg, vg, _ = hc.read_vertices()
+        assert rel_l2(xg, xo) < RUN_TOL
+        assert rel_l2(vg, vo) < RUN_TOL
+        _, ug = hc.read_fluid()
+        _, uo = o.read_fluid()
+        assert rel_l2(ug, uo) < RUN_TOL
+        hc.close()
+
+
+def test_timescale_separation(built):
+    case = mixed_box(wall=False)
+    o = _orc().apply_case(case)
+    hc = case.build()
+    hc.setMaterialTimeScaleSeparation([4, 2, 4], velocity_every=2)
+    o.set_timescales([4, 2, 4], 2)
+    hc.iterate(40)
+    o.step(40)
+    xg, vg, fg = hc.read_vertices()
+    xo, vo, fo = o.read_vertices()
+    assert rel_l2(xg, xo) < RUN_TOL
+    assert rel_l2(vg, vo) < RUN_TOL
+    assert rel_l2(fg, fo) < 1e-8
+    hc.close()
+
+
+def test_mixed_form_error_vs_fp64(built):
+    """FP32 form (f_i - w_i storage) against the FP64 oracle: velocity and
+    positions within 1e-4 relative L2 after 200 steps of a sheared RBC."""
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    case = C.shear_single_rbc(n=24, shear_rate=20000.0, seed=7, min_triangles=320)
+    hc = case.build(form=L.HC_FORM_MIXED_F32)
+    o = _orc().apply_case(case)
+    hc.iterate(200)
+    o.step(200)
+    _, ug = hc.read_fluid()
+    _, uo = o.read_fluid()
+    xg, vg, _ = hc.read_vertices()
+    xo, vo, _ = o.read_vertices()
+    assert rel_l2(ug, uo) < 1e-4
+    assert rel_l2(vg, vo) < 1e-4
+    assert rel_l2(xg, xo) < 1e-6
+    hc.close()
+
+
+def test_error_paths(built):
+    from hemocell_gb300 import HemoCellError, _lib as L
+    case = mixed_box()
+    hc = case.build()
+    with pytest.raises(HemoCellError):
+        hc.setMaterialTimeScaleSeparation([3, 2, 4], velocity_every=2)
+    with pytest.raises(HemoCellError):
+        hc.set_wall_velocity(99, (0, 0, 0))
+    with pytest.raises(HemoCellError):
+        hc.stage(42)
+    hc.close()
