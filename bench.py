@@ -65,7 +65,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -108,7 +108,8 @@ def build_case(steps: int):
 def time_form(case, form, launch, steps, warmup, tune_cache):
     from hemocell_gb300 import _lib as L
     hc = case.build(form=form, launch=launch)
-    hc.autotune(tune_cache)
+    if tune_cache is not None:
+        hc.autotune(tune_cache)
     hc.iterate(warmup)
     hc.sync()
     with ClockSampler() as cs:
@@ -192,11 +193,12 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain form")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -216,7 +218,7 @@ def main():
     from hemocell_gb300 import _lib as L
     case = build_case(args.steps)
     fluid = int((case.flags_array() == 0).sum())
-    tune_cache = os.path.join(ROOT, "hemocell_gb300", "_build", "tuning.txt")
+    tune_cache = None if args.no_autotune else os.path.join(ROOT, "hemocell_gb300", "_build", "tuning.txt")
 
     if world > 1:
         torch.distributed.barrier()

@@ -75,6 +75,7 @@ SIGNATURES = {
     "hc_add_cells": (C.c_int, [P, C.c_int, C.c_int, D, D]),
     "hc_add_cells_xyz": (C.c_int, [P, C.c_int, C.c_int, D]),
     "hc_set_timescales": (C.c_int, [P, I, C.c_int, C.c_int]),
+    "hc_set_vertex_forces": (C.c_int, [P, C.c_int, I, D]),
     "hc_step": (C.c_int, [P, C.c_int]),
     "hc_stage": (C.c_int, [P, C.c_int]),
     "hc_sync": (C.c_int, [P]),

@@ -50,6 +50,31 @@ def _compile(unit: str, hdr_mtime: float, verbose: bool) -> str:
     return obj
 
 
+EXAMPLES = {"oneCellShear": os.path.join(HERE, "cpp", "examples", "oneCellShear", "oneCellShear.cpp")}
+
+
+def build_examples(verbose: bool = False) -> dict:
+    """Compile the C++ case programs written against cpp/hemocell.h."""
+    out = {}
+    for name, src in EXAMPLES.items():
+        exe = os.path.join(BUILD, name)
+        deps = [src, os.path.join(HERE, "cpp", "hemocell.h"), os.path.join(HERE, "cpp", "config.h"), LIB]
+        if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
+            cmd = ["g++", "-std=c++17", "-O2", "-o", exe, src, "-I", os.path.join(_cuda_home(), "include"),
+                   "-L", HERE, "-lhcgpu", f"-Wl,-rpath,{HERE}"]
+            if verbose:
+                print(" ".join(cmd), file=sys.stderr)
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"example {name} failed to build:\n{r.stdout}\n{r.stderr}")
+        out[name] = exe
+    return out
+
+
+def _cuda_home() -> str:
+    return os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
 def build(verbose: bool = False) -> str:
     """Compile every unit and link libhcgpu.so; returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
@@ -62,6 +87,7 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_examples(verbose)
     return LIB
 
 

@@ -203,6 +203,37 @@ def kolmogorov_mix(n: int = 128, rbc_fraction: float = 0.30, n_wbc: int = 2, plt
                 types=types, cells=cells, steps=steps)
 
 
+def stretch_cell(min_triangles: int = 600) -> Case:
+    """Single RBC in a closed 52x26x26 box (tests/validation/stretch_cell):
+    nuP 1.1e-6, dt 1e-7 -> tau 1.82; box faces are static walls; the cell is
+    centred at (12, 6, 6) um with its disc in the x-y plane (axial = x,
+    transverse = y as the test measures them)."""
+    nz = 26
+    dims = (2 * nz, nz, nz)
+    flags = np.zeros((dims[2], dims[1], dims[0]), np.uint8)
+    flags[0, :, :] = flags[-1, :, :] = 1
+    flags[:, 0, :] = flags[:, -1, :] = 1
+    flags[:, :, 0] = flags[:, :, -1] = 1
+    t = rbc_type(min_triangles)
+    xyz = place_cells(t.mesh, np.array([[24.0, 12.0, 12.0]]), np.zeros((1, 3)))
+    tau = 3.0 * 1.1e-6 * DT / DX ** 2 + 0.5
+    return Case("stretch_cell", dims, (0, 0, 0), tau=tau, flags=flags.reshape(-1), walls={1: (0.0, 0.0, 0.0)},
+                types=[t], cells=[(0, xyz)], steps=10000)
+
+
+def stretch_forces(xyz: np.ndarray, force_pN: float, n_forced: int = 7):
+    """HemoCellStretch (helper/hemoCellStretch.cpp:30-78): the n lowest-x
+    vertices get -F/n along x, the n highest-x +F/n; returns (ids, forces)."""
+    df = RHO_P * DX ** 4 / DT ** 2
+    f = force_pN * 1e-12 / df / n_forced
+    order = np.argsort(xyz[:, 0], kind="stable")
+    ids = np.concatenate([order[:n_forced], order[::-1][:n_forced]]).astype(np.int32)
+    forces = np.zeros((2 * n_forced, 3))
+    forces[:n_forced, 0] = -f
+    forces[n_forced:, 0] = f
+    return ids, forces
+
+
 def _mesh_volume(m: Mesh) -> float:
     v0, v1, v2 = (m.xyz[m.tris[:, k]] for k in range(3))
     return float(np.einsum("ij,ij->i", v0, np.cross(v1, v2)).sum() / 6.0)

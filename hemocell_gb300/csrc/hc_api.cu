@@ -51,6 +51,9 @@ struct hc_handle {
   int cur = 0;
   uint32_t* nbmask = nullptr;
   uint8_t* flag = nullptr;
+  uint32_t* ntag = nullptr;
+  void* unode = nullptr;
+  uint32_t* stamp = nullptr;
   void* bodyz = nullptr;
   std::vector<uint8_t> hflag;
   double uw[hcd::MAX_WALL_CLASSES][3];
@@ -94,6 +97,10 @@ struct hc_handle {
   long long device_bytes = 0;
   double* scratch = nullptr;  // readback staging
   size_t scratch_bytes = 0;
+  // external vertex forces (HemoCellStretch)
+  int next = 0, next_cap = 0;
+  int* ext_ids = nullptr;
+  double* ext_f = nullptr;
 };
 
 namespace {
@@ -146,6 +153,9 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   L.nbmask = h->nbmask;
   L.flag = h->flag;
   L.bodyz = (const T*)h->bodyz;
+  L.ntag = h->ntag;
+  L.unode = (T*)h->unode;
+  L.stamp = h->stamp;
   L.omega = (T)(1.0 / h->u.tau);
   for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
@@ -355,6 +365,8 @@ int upload_cell_lists(hc_handle* h) {
 // ----- stage launchers (enqueue only) -------------------------------------
 template <typename T>
 int enq_spread(hc_handle* h) {
+  if (h->next > 0)
+    HC_CUDA(h, hcd::launch_add_vertex_forces<T>(vertex_view<T>(h), h->ext_ids, h->ext_f, h->next, h->stream));
   LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
   HC_CUDA(h, hcd::launch_spread<T>(L, vertex_view<T>(h), h->u.f_limit, h->tune[2], h->stream));
   return HC_OK;
@@ -368,10 +380,16 @@ int enq_collide(hc_handle* h) {
   return HC_OK;
 }
 
-// post-stream view: populations f[cur], force of the last collision F[1-cur]
+// post-stream view: populations f[cur], force of the last collision F[1-cur].
+// The stencil nodes were tagged by this step's spread; a standalone
+// interpolation stage tags them itself (mark = 1).
 template <typename T>
-int enq_interp_advance(hc_handle* h, int do_interp, int do_advance) {
+int enq_interp_advance(hc_handle* h, int do_interp, int do_advance, int mark = 0) {
   LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
+  if (do_interp) {
+    if (mark) HC_CUDA(h, hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream));
+    HC_CUDA(h, hcd::launch_node_velocity<T>(L, h->stream));
+  }
   HC_CUDA(h, hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, do_interp, do_advance, h->tune[3],
                                            h->stream));
   return HC_OK;
@@ -479,7 +497,7 @@ int run_stage(hc_handle* h, int stage) {
     case HC_STAGE_COLLIDE_STREAM:
       return enq_collide<T>(h);
     case HC_STAGE_INTERPOLATE:
-      return enq_interp_advance<T>(h, 1, 0);
+      return enq_interp_advance<T>(h, 1, 0, 1);
     case HC_STAGE_ADVANCE:
       return enq_interp_advance<T>(h, 0, 1);
     case HC_STAGE_MECHANICS:
@@ -623,6 +641,8 @@ float time_it(hc_handle* h, int reps, int which) {
       hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream);
     } else if (which == 1) {
       LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
+      hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream);
+      hcd::launch_node_velocity<T>(L, h->stream);
       hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, 1, 0, h->tune[3], h->stream);
     } else {
       enq_mechanics<T>(h, true);
@@ -836,6 +856,17 @@ hc_handle* hc_create(const hc_params* p) {
     cudaMemsetAsync(h->f[k], 0, fb, h->stream);
     cudaMemsetAsync(h->F[k], 0, Fb, h->stream);
   }
+  if (dalloc(h, (void**)&h->ntag, 4 * h->N) != cudaSuccess || dalloc(h, &h->unode, 3 * h->ts * h->N) != cudaSuccess ||
+      dalloc(h, (void**)&h->stamp, 4) != cudaSuccess)
+    return bail("out of device memory (node tags)");
+  cudaMemsetAsync(h->ntag, 0, 4 * h->N, h->stream);
+  cudaMemsetAsync(h->unode, 0, 3 * h->ts * h->N, h->stream);
+  {
+    const uint32_t one = 1;
+    cudaMemcpyAsync(h->stamp, &one, 4, cudaMemcpyHostToDevice, h->stream);
+  }
+  if ((e = h->f64 ? hcd::prepare_spread<double>() : hcd::prepare_spread<float>()) != cudaSuccess)
+    return bail(std::string("spread attributes: ") + cudaGetErrorString(e));
   if (dalloc(h, (void**)&h->nbmask, 4 * h->N) != cudaSuccess || dalloc(h, (void**)&h->flag, h->N) != cudaSuccess ||
       dalloc(h, &h->bodyz, 3 * h->ts * h->nz) != cudaSuccess ||
       dalloc(h, (void**)&h->dtypes, sizeof(TypeDev) * hcd::MAX_TYPES) != cudaSuccess ||
@@ -861,10 +892,11 @@ int hc_destroy(hc_handle* h) {
     dfree(ts.blob);
     dfree(ts.dcells);
   }
-  void* ptrs[] = {h->nbmask, h->flag,  h->bodyz,     h->dtypes,     h->x,          h->v,
+  void* ptrs[] = {h->ntag, h->unode, h->stamp, h->nbmask, h->flag,  h->bodyz,     h->dtypes,     h->x,          h->v,
                   h->fv,     h->vcell, h->vnode,     h->vtile,      h->cell_type,  h->cell_voff,
                   h->alive,  h->dcells_all, h->status, h->bin_counts, h->bin_cursor, h->bin_offsets,
-                  h->tile_vertices, h->tile_cell_counts, h->tile_cell_offsets, h->tile_cells, h->scratch};
+                  h->tile_vertices, h->tile_cell_counts, h->tile_cell_offsets, h->tile_cells, h->scratch,
+                  h->ext_ids, h->ext_f};
   for (void* q : ptrs) dfree(q);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1045,6 +1077,29 @@ int hc_set_timescales(hc_handle* h, const int* every, int ntypes, int velocity_e
   }
   for (int t = 0; t < ntypes; ++t) h->types[t].every = every[t];
   h->velocity_every = velocity_every;
+  invalidate_graph(h);
+  return HC_OK;
+}
+
+int hc_set_vertex_forces(hc_handle* h, int n, const int* ids, const double* forces) {
+  if (!h || n < 0 || (n > 0 && (!ids || !forces))) return HC_ERR_INVALID;
+  for (int k = 0; k < n; ++k)
+    if (ids[k] < 0 || ids[k] >= h->nvert) return fail(h, HC_ERR_INVALID, "vertex id out of range");
+  if (n > h->next_cap) {
+    dfree(h->ext_ids);
+    dfree(h->ext_f);
+    h->ext_ids = nullptr;
+    h->ext_f = nullptr;
+    HC_CUDA(h, dalloc(h, (void**)&h->ext_ids, sizeof(int) * n));
+    HC_CUDA(h, dalloc(h, (void**)&h->ext_f, sizeof(double) * 3 * n));
+    h->next_cap = n;
+  }
+  if (n > 0) {
+    HC_CUDA(h, cudaMemcpyAsync(h->ext_ids, ids, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+    HC_CUDA(h, cudaMemcpyAsync(h->ext_f, forces, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  h->next = n;
   invalidate_graph(h);
   return HC_OK;
 }

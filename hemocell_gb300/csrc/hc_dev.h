@@ -28,6 +28,9 @@ struct LbmView {
   const uint32_t* __restrict__ nbmask;
   const uint8_t* __restrict__ flag;
   const T* __restrict__ bodyz;  // [3][nz]
+  uint32_t* ntag;                // per node: stamp of the last step whose stencils touch it
+  T* unode;                      // [3][N] velocity of tagged nodes
+  uint32_t* stamp;               // device step stamp (advanced by interp_advance)
   T omega;
   T uw[MAX_WALL_CLASSES][3];
 };
@@ -89,8 +92,17 @@ template <typename T>
 cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs,
                           cudaStream_t s);
 template <typename T>
+cudaError_t prepare_spread();
+template <typename T>
+cudaError_t launch_add_vertex_forces(const VertexView<T>& vv, const int* ids, const double* fext, int n,
+                                     cudaStream_t s);
+template <typename T>
 cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg,
                                   int do_interp, int do_advance, int bs, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s);
+template <typename T>
+cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s);
 template <typename T>
 cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s);
 template <typename T>

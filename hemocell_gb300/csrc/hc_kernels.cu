@@ -264,45 +264,147 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
 
 // ---------------------------------------------------------------------------
 // K2: spreadParticleForce (core/hemoCellParticleField.cpp:841-863) with the
-// FORCE_LIMIT clamp written back (:847-852).
+// FORCE_LIMIT clamp written back (:847-852).  The contributions of a CTA's
+// vertices are first summed per node in a shared-memory hash table (open
+// addressing, at most half full), then each distinct node gets one global
+// atomic per component.  The stencil nodes are tagged with the step stamp
+// so the interpolation computes node velocities only where needed.
+constexpr int SPREAD_BS = 128;
+constexpr int SPREAD_HASH = 2048;  // >= 2 * 8 * SPREAD_BS
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const VertexView<T> vv, const T f_limit) {
+__global__ void __launch_bounds__(SPREAD_BS) k_spread(const LbmView<T> L, const VertexView<T> vv, const T f_limit) {
+  extern __shared__ double spread_smem[];
+  int* hkey = reinterpret_cast<int*>(spread_smem);
+  T* hval = reinterpret_cast<T*>(hkey + SPREAD_HASH);  // [3][SPREAD_HASH]
+  for (int k = threadIdx.x; k < SPREAD_HASH; k += blockDim.x) {
+    hkey[k] = -1;
+    hval[k] = T(0);
+    hval[SPREAD_HASH + k] = T(0);
+    hval[2 * SPREAD_HASH + k] = T(0);
+  }
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= vv.nvert) return;
-  if (!vv.alive[vv.vcell[i]]) return;
-  const long long V = vv.V;
-  T fx = vv.f[i], fy = vv.f[V + i], fz = vv.f[2 * V + i];
-  T mag = fx * fx;
-  mag += fy * fy;
-  mag += fz * fz;
-  mag = sqrt(mag);
-  if (mag > f_limit) {
-    const T s = f_limit / mag;
-    fx *= s;
-    fy *= s;
-    fz *= s;
-    vv.f[i] = fx;
-    vv.f[V + i] = fy;
-    vv.f[2 * V + i] = fz;
-  }
-  Kern<T> K;
-  ibm_weights(L, vv.x[i], vv.x[V + i], vv.x[2 * V + i], K);
-  T* F = const_cast<T*>(L.Fcur);
+  const uint32_t stamp = *L.stamp;
+  if (i < vv.nvert && vv.alive[vv.vcell[i]]) {
+    const long long V = vv.V;
+    T fx = vv.f[i], fy = vv.f[V + i], fz = vv.f[2 * V + i];
+    T mag = fx * fx;
+    mag += fy * fy;
+    mag += fz * fz;
+    mag = sqrt(mag);
+    if (mag > f_limit) {
+      const T s = f_limit / mag;
+      fx *= s;
+      fy *= s;
+      fz *= s;
+      vv.f[i] = fx;
+      vv.f[V + i] = fy;
+      vv.f[2 * V + i] = fz;
+    }
+    Kern<T> K;
+    ibm_weights(L, vv.x[i], vv.x[V + i], vv.x[2 * V + i], K);
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    if (K.node[j] < 0) continue;
-    atomicAdd(F + K.node[j], fx * K.w[j]);
-    atomicAdd(F + L.N + K.node[j], fy * K.w[j]);
-    atomicAdd(F + 2 * L.N + K.node[j], fz * K.w[j]);
+    for (int j = 0; j < 8; ++j) {
+      if (K.node[j] < 0) continue;
+      const int node = (int)K.node[j];
+      L.ntag[node] = stamp;
+      unsigned h = ((unsigned)node * 2654435761u) & (SPREAD_HASH - 1);
+      for (int probe = 0; probe < SPREAD_HASH; ++probe) {
+        const int old = atomicCAS(hkey + h, -1, node);
+        if (old == -1 || old == node) {
+          atomicAdd(hval + h, fx * K.w[j]);
+          atomicAdd(hval + SPREAD_HASH + h, fy * K.w[j]);
+          atomicAdd(hval + 2 * SPREAD_HASH + h, fz * K.w[j]);
+          break;
+        }
+        h = (h + 1) & (SPREAD_HASH - 1);
+      }
+    }
   }
+  __syncthreads();
+  T* F = const_cast<T*>(L.Fcur);
+  for (int k = threadIdx.x; k < SPREAD_HASH; k += blockDim.x) {
+    const int node = hkey[k];
+    if (node < 0) continue;
+    atomicAdd(F + node, hval[k]);
+    atomicAdd(F + L.N + node, hval[SPREAD_HASH + k]);
+    atomicAdd(F + 2 * L.N + node, hval[2 * SPREAD_HASH + k]);
+  }
+}
+
+// Tag the stencil nodes of every vertex (used when the interpolation runs
+// as a stage of its own, without the spread of the same step).
+template <typename T>
+__global__ void k_mark_nodes(const LbmView<T> L, const VertexView<T> vv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= vv.nvert || !vv.alive[vv.vcell[i]]) return;
+  const uint32_t stamp = *L.stamp;
+  Kern<T> K;
+  ibm_weights(L, vv.x[i], vv.x[vv.V + i], vv.x[2 * vv.V + i], K);
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (K.node[j] >= 0) L.ntag[K.node[j]] = stamp;
+}
+template <typename T>
+cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s) {
+  if (vv.nvert <= 0) return cudaSuccess;
+  k_mark_nodes<T><<<(vv.nvert + 255) / 256, 256, 0, s>>>(L, vv);
+  return cudaGetLastError();
+}
+
+// Velocity of every tagged node from the post-stream populations (L.fsrc)
+// and the force of the collision that produced them (L.Fcur).
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L.N) return;
+  if (L.ntag[n] != *L.stamp) return;
+  T ux, uy, uz;
+  node_velocity(L.fsrc, L.Fcur, L.N, n, ux, uy, uz);
+  L.unode[n] = ux;
+  L.unode[L.N + n] = uy;
+  L.unode[2 * L.N + n] = uz;
+}
+template <typename T>
+cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s) {
+  k_node_velocity<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+// External vertex forces (HemoCellStretch::applyForce adds them to the
+// vertex force right before the spread, helper/hemoCellStretch.cpp:63-78).
+template <typename T>
+__global__ void k_add_vertex_forces(const VertexView<T> vv, const int* ids, const double* fext, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int i = ids[k];
+  if (i < 0 || i >= vv.nvert) return;
+  vv.f[i] += (T)fext[3 * k];
+  vv.f[vv.V + i] += (T)fext[3 * k + 1];
+  vv.f[2 * vv.V + i] += (T)fext[3 * k + 2];
+}
+template <typename T>
+cudaError_t launch_add_vertex_forces(const VertexView<T>& vv, const int* ids, const double* fext, int n,
+                                     cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_add_vertex_forces<T><<<(n + 127) / 128, 128, 0, s>>>(vv, ids, fext, n);
+  return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs, cudaStream_t s) {
   if (vv.nvert <= 0) return cudaSuccess;
-  if (bs <= 0) bs = 128;
-  k_spread<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, (T)f_limit);
+  (void)bs;
+  const size_t smem = SPREAD_HASH * (sizeof(int) + 3 * sizeof(T));
+  k_spread<T><<<(vv.nvert + SPREAD_BS - 1) / SPREAD_BS, SPREAD_BS, smem, s>>>(L, vv, (T)f_limit);
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t prepare_spread() {
+  return cudaFuncSetAttribute(k_spread<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(SPREAD_HASH * (sizeof(int) + 3 * sizeof(T))));
 }
 
 // ---------------------------------------------------------------------------
@@ -314,6 +416,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, const VertexView<T> vv, const TileGrid tg,
                                                         const int do_interp, const int do_advance) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) *L.stamp += 1;  // the next spread tags with a fresh stamp; nothing here reads it
   if (i >= vv.nvert) return;
   const int cell = vv.vcell[i];
   if (!vv.alive[cell]) {
@@ -333,11 +436,9 @@ __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, cons
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       if (K.node[j] < 0) continue;
-      T ux, uy, uz;
-      node_velocity(L.fsrc, L.Fcur, L.N, K.node[j], ux, uy, uz);
-      vx += ux * K.w[j];
-      vy += uy * K.w[j];
-      vz += uz * K.w[j];
+      vx += L.unode[K.node[j]] * K.w[j];
+      vy += L.unode[L.N + K.node[j]] * K.w[j];
+      vz += L.unode[2 * L.N + K.node[j]] * K.w[j];
     }
     vv.v[i] = vx;
     vv.v[V + i] = vy;
@@ -476,6 +577,7 @@ size_t mechanics_smem_bytes(int nv) {
 template <typename T>
 __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
   extern __shared__ double smem_d[];
+  __shared__ TypeDev tshared;
   double* red = smem_d;                  // 34 doubles
   T* sx = reinterpret_cast<T*>(smem_d + 34);
   const VertexView<T>& vv = M.vv;
@@ -484,11 +586,13 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
   constexpr bool kF64 = sizeof(T) == 8;
   for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
     const int cell = M.cells[ci];
-    const TypeDev& t = M.types[M.cell_type[cell]];
+    __syncthreads();  // previous cell fully written out
+    if (tid == 0) tshared = M.types[M.cell_type[cell]];
+    __syncthreads();
+    const TypeDev& t = tshared;
     const int nv = t.nv;
     const int voff = M.cell_voff[cell];
     T* sf = sx + 3 * nv;
-    __syncthreads();  // previous cell fully written out
     const bool alive = vv.alive[cell] != 0;
     // positions: absolute in FP64, relative to vertex 0 in FP32
     const double r0x = kF64 ? 0.0 : vv.x[voff], r0y = kF64 ? 0.0 : vv.x[V + voff],
@@ -537,6 +641,7 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
       const double volume = block_sum<T>(vol, red) * (1.0 / 6.0);
       const double vfr = (volume - t.volume_eq) / t.volume_eq;
       const double vforce = -t.k_volume * vfr / fabs(kMaxVol - vfr * vfr);
+      const double vforce_per_area = vforce / t.area_mean_eq;
       // --- faces: volume force (:103-124)
       for (int k = tid; k < t.nf; k += bs) {
         const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
@@ -555,7 +660,7 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
         if (kF64) {
           lvf = vscale(vscale(n, (T)vforce), area / (T)t.area_mean_eq);
         } else {
-          lvf = vscale(n, (T)(vforce * ((double)area / t.area_mean_eq)));
+          lvf = vscale(n, (T)(vforce_per_area * (double)area));
         }
         add3(sf, i0, lvf);
         add3(sf, i1, lvf);
@@ -935,6 +1040,11 @@ cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, cons
 #define HC_INST(T)                                                                                              \
   template cudaError_t launch_collide_stream<T>(const LbmView<T>&, int, int, cudaStream_t);                    \
   template cudaError_t launch_spread<T>(const LbmView<T>&, const VertexView<T>&, double, int, cudaStream_t);   \
+  template cudaError_t prepare_spread<T>();                                                                    \
+  template cudaError_t launch_mark_nodes<T>(const LbmView<T>&, const VertexView<T>&, cudaStream_t);            \
+  template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                               \
+  template cudaError_t launch_add_vertex_forces<T>(const VertexView<T>&, const int*, const double*, int,       \
+                                                   cudaStream_t);                                              \
   template cudaError_t launch_interp_advance<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&, int, \
                                                 int, int, cudaStream_t);                                       \
   template cudaError_t launch_mechanics<T>(const MechView<T>&, int, int, cudaStream_t);                        \

@@ -244,6 +244,13 @@ class HemoCell:
         e = np.ascontiguousarray(every, np.int32)
         self._check(self._lib.hc_set_timescales(self._h, _ip(e), len(e), velocity_every))
 
+    def set_vertex_forces(self, ids, forces):
+        """Constant external vertex forces added before every spread (HemoCellStretch)."""
+        ids = np.ascontiguousarray(ids, np.int32).reshape(-1)
+        forces = np.ascontiguousarray(forces, np.float64).reshape(-1, 3)
+        self._check(self._lib.hc_set_vertex_forces(self._h, len(ids), _ip(ids) if len(ids) else None,
+                                                   _dp(forces) if len(ids) else None))
+
     # --- stepping
     def iterate(self, nsteps: int = 1):
         self._check(self._lib.hc_step(self._h, nsteps))

@@ -121,6 +121,11 @@ int hc_add_cells_xyz(hc_handle* h, int type, int n, const double* xyz);
  * (hemocell.h:150,159; checked as in core/hemoCell.cpp:620-627) */
 int hc_set_timescales(hc_handle* h, const int* material_every, int ntypes, int velocity_every);
 
+/* HemoCellStretch::applyForce (helper/hemoCellStretch.cpp:63-78): a constant
+ * external force added to the listed vertices' force before every spread
+ * (ids are global vertex indices, forces n*3 in lattice units); n = 0 clears */
+int hc_set_vertex_forces(hc_handle* h, int n, const int* ids, const double* forces);
+
 /* --- the hot path: HemoCell::iterate() (core/hemoCell.cpp:299-376) */
 int hc_step(hc_handle* h, int nsteps);
 int hc_stage(hc_handle* h, int stage); /* one stage, for stage-wise parity */

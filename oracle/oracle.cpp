@@ -263,6 +263,7 @@ struct orc_sim {
   std::vector<int> material_every;
   int velocity_every = 1;
   int iter = 0;
+  std::vector<std::pair<int, V3>> ext;  // external vertex forces
   // IBM kernel cache of the last spread (core/hemoCellParticle.h:75-76)
   std::vector<std::vector<std::pair<long, double>>> kern;
 
@@ -415,6 +416,7 @@ void kernelWeights(const orc_sim* s, V3 p, std::vector<std::pair<long, double>>&
 void spread(orc_sim* s) {
   const long N = s->N;
   const int V = (int)s->x.size();
+  for (const auto& e : s->ext) s->fv[e.first] += e.second;
   s->kern.resize(V);
   for (int i = 0; i < V; ++i) {
     if (!s->cells[s->vcell[i]].alive) { s->kern[i].clear(); continue; }
@@ -811,6 +813,11 @@ int orc_add_cell(orc_sim* s, int type, const double* xyz) {
 void orc_set_timescales(orc_sim* s, const int* material_every, int velocity_every) {
   for (size_t i = 0; i < s->material_every.size(); ++i) s->material_every[i] = material_every[i];
   s->velocity_every = velocity_every;
+}
+
+void orc_set_vertex_forces(orc_sim* s, int n, const int* ids, const double* forces) {
+  s->ext.clear();
+  for (int k = 0; k < n; ++k) s->ext.push_back({ids[k], V3{forces[3 * k], forces[3 * k + 1], forces[3 * k + 2]}});
 }
 
 void orc_stage_spread(orc_sim* s) { spread(s); }

@@ -61,6 +61,9 @@ int orc_add_cell_type(orc_sim* s, int model, int nv, const double* xyz,
                       const double* k);
 int orc_add_cell(orc_sim* s, int type, const double* xyz);
 void orc_set_timescales(orc_sim* s, const int* material_every, int velocity_every);
+/* constant external vertex forces added before each spread
+ * (HemoCellStretch::applyForce, helper/hemoCellStretch.cpp:63-78) */
+void orc_set_vertex_forces(orc_sim* s, int n, const int* ids, const double* forces);
 
 /* Stepping --------------------------------------------------------------- */
 void orc_step(orc_sim* s, int nsteps);

@@ -32,6 +32,7 @@ _SIG = {
     "orc_add_cell_type": (C.c_int, [P, C.c_int, C.c_int, D, C.c_int, I, C.c_int, I, D]),
     "orc_add_cell": (C.c_int, [P, C.c_int, D]),
     "orc_set_timescales": (None, [P, I, C.c_int]),
+    "orc_set_vertex_forces": (None, [P, C.c_int, I, D]),
     "orc_step": (None, [P, C.c_int]),
     "orc_stage_spread": (None, [P]),
     "orc_stage_collide_stream": (None, [P]),
@@ -145,6 +146,11 @@ class Oracle:
     def set_timescales(self, every, velocity_every=1):
         e = np.ascontiguousarray(every, np.int32)
         self.L.orc_set_timescales(self.s, _i(e), velocity_every)
+
+    def set_vertex_forces(self, ids, forces):
+        ids = np.ascontiguousarray(ids, np.int32).reshape(-1)
+        forces = np.ascontiguousarray(forces, np.float64).reshape(-1, 3)
+        self.L.orc_set_vertex_forces(self.s, len(ids), _i(ids), _d(forces))
 
     def step(self, n=1):
         self.L.orc_step(self.s, n)

@@ -202,28 +202,63 @@ def test_full_step_shear_rbc(built):
     hc.close()
 
 
+def mixed_periodic(seed=9):
+    """Periodic 40x36x32 box with one RBC, two PLTs and one WBC, not
+    overlapping, a uniform body force: the batched/graph path end to end."""
+    C = _cases()
+    n = (40, 36, 32)
+    types = [C.rbc_type(600), C.plt_type(320), C.wbc_type(1280)]
+    rng = np.random.default_rng(seed)
+    place = [(0, (11.0, 10.0, 16.0)), (1, (30.0, 8.0, 6.0)), (1, (30.0, 28.0, 26.0)), (2, (28.0, 22.0, 15.0))]
+    cells = []
+    for t, c in place:
+        ang = rng.uniform(-np.pi, np.pi, size=(1, 3))
+        cells.append((t, C.place_cells(types[t].mesh, np.array([c]), ang)))
+    return C.Case("mixed_periodic", n, (1, 1, 1), types=types, cells=cells, body_mode=1, body=(2e-6, -1e-6, 5e-7))
+
+
+def _per_type_errors(case, a, b):
+    out, k = {}, 0
+    for t, xyz in case.cells:
+        n = xyz.shape[0]
+        out.setdefault(t, []).append(rel_l2(a[k:k + n], b[k:k + n]))
+        k += n
+    return {t: max(v) for t, v in out.items()}
+
+
 def test_full_step_mixed_types_batched_graph(built):
     from hemocell_gb300 import _lib as L
-    case = mixed_box(wall=False)
+    case = mixed_periodic()
     o = _orc().apply_case(case)
     hp = case.build(launch=L.HC_LAUNCH_PER_STAGE)
     hb = case.build(launch=L.HC_LAUNCH_BATCHED)
-    hp.iterate(100)
-    hb.iterate(100)  # graph replay (2 steps per launch)
-    o.step(100)
-    xo, vo, _ = o.read_vertices()
+    errs = []
+    for chunk in (10, 40, 50):
+        hp.iterate(chunk)
+        hb.iterate(chunk)  # graph replay (2 steps per launch)
+        o.step(chunk)
+        xo, vo, _ = o.read_vertices()
+        for name, hc in (("per_stage", hp), ("batched", hb)):
+            xg, vg, _ = hc.read_vertices()
+            errs.append((o_iter(o), name, rel_l2(xg, xo), rel_l2(vg, vo), _per_type_errors(case, vg, vo)))
+    msg = "\n".join(map(str, errs))
+    print(msg)
+    for it, name, ex, ev, _ in errs:
+        assert ex < RUN_TOL, msg
+        assert ev < RUN_TOL, msg
+    _, uo = o.read_fluid()
     for hc in (hp, hb):
-        xg, vg, _ = hc.read_vertices()
-        assert rel_l2(xg, xo) < RUN_TOL
-        assert rel_l2(vg, vo) < RUN_TOL
         _, ug = hc.read_fluid()
-        _, uo = o.read_fluid()
         assert rel_l2(ug, uo) < RUN_TOL
         hc.close()
 
 
+def o_iter(o):
+    return o.L.orc_iter(o.s)
+
+
 def test_timescale_separation(built):
-    case = mixed_box(wall=False)
+    case = mixed_periodic()
     o = _orc().apply_case(case)
     hc = case.build()
     hc.setMaterialTimeScaleSeparation([4, 2, 4], velocity_every=2)
