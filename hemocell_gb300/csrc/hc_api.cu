@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <sstream>
 #include <string>
@@ -232,35 +233,6 @@ int upload_flags(hc_handle* h) {
   return HC_OK;
 }
 
-template <typename T>
-__global__ void k_fill_body(T* F, const T* bodyz, long long plane, int nz, long long N) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  const int z = (int)(n / plane);
-  F[n] = bodyz[z];
-  F[N + n] = bodyz[nz + z];
-  F[2 * N + n] = bodyz[2 * nz + z];
-}
-
-template <typename T>
-__global__ void k_init_eq(T* f, const uint8_t* flag, long long N, double rho, double ux, double uy, double uz) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
-  const int C[19][3] = {{0, 0, 0},  {-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {-1, -1, 0}, {-1, 1, 0}, {-1, 0, -1},
-                        {-1, 0, 1}, {0, -1, -1}, {0, -1, 1}, {1, 0, 0}, {0, 1, 0},  {0, 0, 1},  {1, 1, 0},
-                        {1, -1, 0}, {1, 0, 1},  {1, 0, -1}, {0, 1, 1}, {0, 1, -1}};
-  const double uu = ux * ux + uy * uy + uz * uz;
-  for (int i = 0; i < 19; ++i) {
-    double w = i == 0 ? 1.0 / 3.0 : ((i - 1) % 9 < 3 ? 1.0 / 18.0 : 1.0 / 36.0);
-    double v = 0.0;
-    if (flag[n] == 0) {
-      const double cu = C[i][0] * ux + C[i][1] * uy + C[i][2] * uz;
-      v = w * ((rho - 1.0) + rho * (3.0 * cu + 4.5 * cu * cu - 1.5 * uu));
-    }
-    f[i * N + n] = (T)v;
-  }
-}
-
 int upload_body(hc_handle* h) {
   std::vector<double> bz(3 * h->nz, 0.0);
   for (int z = 0; z < h->nz; ++z) {
@@ -270,17 +242,19 @@ int upload_body(hc_handle* h) {
       bz[z] = h->body[0] * std::sin(2.0 * M_PI * (double)z / (double)h->nz);
     }
   }
+  const long long plane = (long long)h->nx * h->ny;
   if (h->f64) {
     HC_CUDA(h, cudaMemcpyAsync(h->bodyz, bz.data(), 8 * bz.size(), cudaMemcpyHostToDevice, h->stream));
-    k_fill_body<double><<<(unsigned)((h->N + 255) / 256), 256, 0, h->stream>>>(
-        (double*)h->F[h->cur], (const double*)h->bodyz, (long long)h->nx * h->ny, h->nz, h->N);
+    HC_CUDA(h, hcd::launch_fill_body<double>((double*)h->F[h->cur], (const double*)h->bodyz, plane, h->nz, h->N,
+                                             h->stream));
   } else {
     std::vector<float> bf(bz.begin(), bz.end());
     HC_CUDA(h, cudaMemcpyAsync(h->bodyz, bf.data(), 4 * bf.size(), cudaMemcpyHostToDevice, h->stream));
-    k_fill_body<float><<<(unsigned)((h->N + 255) / 256), 256, 0, h->stream>>>(
-        (float*)h->F[h->cur], (const float*)h->bodyz, (long long)h->nx * h->ny, h->nz, h->N);
+    HC_CUDA(h, hcd::launch_fill_body<float>((float*)h->F[h->cur], (const float*)h->bodyz, plane, h->nz, h->N,
+                                            h->stream));
+    // the pageable source of an async copy must outlive it
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
   }
-  HC_CUDA(h, cudaGetLastError());
   return HC_OK;
 }
 
@@ -590,23 +564,13 @@ int add_cells_positions(hc_handle* h, int type, int n, const std::vector<double>
   return upload_cell_lists(h);
 }
 
-template <typename T>
-__global__ void k_soa_to_aos(const T* src, double* dst, long long V, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  dst[3 * (long long)i] = (double)src[i];
-  dst[3 * (long long)i + 1] = (double)src[V + i];
-  dst[3 * (long long)i + 2] = (double)src[2 * V + i];
-}
-
 // device [3][Vcap] (T) -> host [V][3] double: transpose on the device, then
 // one D2H copy straight into the caller's buffer
 template <typename T>
 int read3(hc_handle* h, const void* src, double* out) {
   int rc;
   if ((rc = ensure_scratch(h, sizeof(double) * 3 * std::max<int>(1, h->nvert))) != HC_OK) return rc;
-  k_soa_to_aos<T><<<(h->nvert + 255) / 256, 256, 0, h->stream>>>((const T*)src, h->scratch, h->Vcap, h->nvert);
-  HC_CUDA(h, cudaGetLastError());
+  HC_CUDA(h, hcd::launch_soa_to_aos<T>((const T*)src, h->scratch, h->Vcap, h->nvert, h->stream));
   HC_CUDA(h, cudaMemcpyAsync(out, h->scratch, 8 * 3 * (size_t)h->nvert, cudaMemcpyDeviceToHost, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
@@ -623,7 +587,7 @@ int write3(hc_handle* h, void* dst, size_t es, const double* in) {
     int rc;
     if ((rc = ensure_scratch(h, sizeof(double) * 3 * V)) != HC_OK) return rc;
     HC_CUDA(h, cudaMemcpyAsync(h->scratch, buf.data(), 8 * 3 * V, cudaMemcpyHostToDevice, h->stream));
-    HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)dst, 3 * V, 0.0, 1, h->stream));
+    HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)dst, 3 * V, h->stream));
   }
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
@@ -725,8 +689,9 @@ int autotune(hc_handle* h, const char* cache) {
     int mb = h->tune[4], mg = h->tune[5];
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
-    for (int bs : {128, 256, 512})
+    for (int bs : {128, 256, 512, 1024})
       for (int gr : {0, 2 * sms, 4 * sms}) {
+        if (bs > 512 && h->f64) continue;
         if (gr != 0 && h->p.launch != HC_LAUNCH_BATCHED) continue;
         h->tune[4] = bs;
         h->tune[5] = gr;
@@ -783,6 +748,22 @@ int profile_stages(hc_handle* h, int nsteps, double* out) {
   }
   for (auto& e : ev) cudaEventDestroy(e);
   for (int s = 0; s < 5; ++s) out[s] = nsteps > 0 ? acc[s] / nsteps : 0.0;
+  return HC_OK;
+}
+
+// The stored state is post-collision; the walls decide how it is pulled.
+// Changing them re-stores the current post-stream populations so that the
+// fluid state itself is unchanged.
+int restore_populations(hc_handle* h, const std::function<int()>& change) {
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 19 * h->N)) != HC_OK) return rc;
+  if (h->f64) HC_CUDA(h, hcd::launch_stream_out<double>(lbm_view<double>(h, h->cur, h->cur), h->scratch, h->stream));
+  else HC_CUDA(h, hcd::launch_stream_out<float>(lbm_view<float>(h, h->cur, h->cur), h->scratch, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if ((rc = change()) != HC_OK) return rc;
+  if (h->f64) HC_CUDA(h, hcd::launch_stream_in<double>(lbm_view<double>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
+  else HC_CUDA(h, hcd::launch_stream_in<float>(lbm_view<float>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
 }
 
@@ -849,24 +830,23 @@ hc_handle* hc_create(const hc_params* p) {
   if (e != cudaSuccess) return bail(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(std::string("stream: ") + cudaGetErrorString(e));
-  const size_t fb = 19 * h->ts * (size_t)h->N, Fb = 3 * h->ts * (size_t)h->N;
+  const size_t fb = 19 * h->ts * (size_t)h->N;
+  const size_t Fb = h->f64 ? hcd::field_bytes<double>(h->N) : hcd::field_bytes<float>(h->N);
   for (int k = 0; k < 2; ++k) {
     if ((e = dalloc(h, &h->f[k], fb)) != cudaSuccess) return bail("out of device memory (populations)");
     if ((e = dalloc(h, &h->F[k], Fb)) != cudaSuccess) return bail("out of device memory (force field)");
     cudaMemsetAsync(h->f[k], 0, fb, h->stream);
     cudaMemsetAsync(h->F[k], 0, Fb, h->stream);
   }
-  if (dalloc(h, (void**)&h->ntag, 4 * h->N) != cudaSuccess || dalloc(h, &h->unode, 3 * h->ts * h->N) != cudaSuccess ||
+  if (dalloc(h, (void**)&h->ntag, 4 * h->N) != cudaSuccess || dalloc(h, &h->unode, Fb) != cudaSuccess ||
       dalloc(h, (void**)&h->stamp, 4) != cudaSuccess)
     return bail("out of device memory (node tags)");
   cudaMemsetAsync(h->ntag, 0, 4 * h->N, h->stream);
-  cudaMemsetAsync(h->unode, 0, 3 * h->ts * h->N, h->stream);
+  cudaMemsetAsync(h->unode, 0, Fb, h->stream);
   {
     const uint32_t one = 1;
     cudaMemcpyAsync(h->stamp, &one, 4, cudaMemcpyHostToDevice, h->stream);
   }
-  if ((e = h->f64 ? hcd::prepare_spread<double>() : hcd::prepare_spread<float>()) != cudaSuccess)
-    return bail(std::string("spread attributes: ") + cudaGetErrorString(e));
   if (dalloc(h, (void**)&h->nbmask, 4 * h->N) != cudaSuccess || dalloc(h, (void**)&h->flag, h->N) != cudaSuccess ||
       dalloc(h, &h->bodyz, 3 * h->ts * h->nz) != cudaSuccess ||
       dalloc(h, (void**)&h->dtypes, sizeof(TypeDev) * hcd::MAX_TYPES) != cudaSuccess ||
@@ -918,17 +898,21 @@ int hc_derived_units(const hc_handle* h, double* out) {
 
 int hc_set_flags(hc_handle* h, const uint8_t* flags) {
   if (!h || !flags) return HC_ERR_INVALID;
-  std::memcpy(h->hflag.data(), flags, h->N);
   invalidate_graph(h);
-  return upload_flags(h);
+  return restore_populations(h, [&]() {
+    std::memcpy(h->hflag.data(), flags, h->N);
+    return upload_flags(h);
+  });
 }
 
 int hc_set_wall_velocity(hc_handle* h, int cls, const double* u3) {
   if (!h || !u3) return HC_ERR_INVALID;
   if (cls < 0 || cls >= hcd::MAX_WALL_CLASSES) return fail(h, HC_ERR_INVALID, "wall class out of range [0,16)");
-  for (int a = 0; a < 3; ++a) h->uw[cls][a] = u3[a];
   invalidate_graph(h);
-  return HC_OK;
+  return restore_populations(h, [&]() {
+    for (int a = 0; a < 3; ++a) h->uw[cls][a] = u3[a];
+    return HC_OK;
+  });
 }
 
 int hc_set_body_force(hc_handle* h, int mode, const double* p) {
@@ -944,11 +928,9 @@ int hc_set_body_force(hc_handle* h, int mode, const double* p) {
 int hc_init_equilibrium(hc_handle* h, double rho, const double* u3) {
   if (!h) return HC_ERR_INVALID;
   if (!(rho > 0)) return fail(h, HC_ERR_INVALID, "density must be positive");
-  const double ux = u3 ? u3[0] : 0, uy = u3 ? u3[1] : 0, uz = u3 ? u3[2] : 0;
-  const unsigned g = (unsigned)((h->N + 255) / 256);
-  if (h->f64) k_init_eq<double><<<g, 256, 0, h->stream>>>((double*)h->f[h->cur], h->flag, h->N, rho, ux, uy, uz);
-  else k_init_eq<float><<<g, 256, 0, h->stream>>>((float*)h->f[h->cur], h->flag, h->N, rho, ux, uy, uz);
-  HC_CUDA(h, cudaGetLastError());
+  // post-collision values whose pull is the equilibrium of (rho, u)
+  if (h->f64) HC_CUDA(h, hcd::launch_stream_in<double>(lbm_view<double>(h, 1 - h->cur, h->cur), nullptr, rho, u3, h->stream));
+  else HC_CUDA(h, hcd::launch_stream_in<float>(lbm_view<float>(h, 1 - h->cur, h->cur), nullptr, rho, u3, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
 }
@@ -1001,12 +983,15 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
   };
   const size_t o_a0 = put_d(c.tri_a0), o_l0 = put_d(c.edge_l0), o_ang = put_d(c.edge_angle0),
                o_pd = put_d(c.patch_d0), o_il = put_d(c.inner_l0);
-  const size_t ib = 4 * iv.size(), db = 8 * std::max<size_t>(dv.size(), 1);
-  HC_CUDA(h, dalloc(h, &ts.blob, ib + db));
+  std::vector<float> fv(dv.begin(), dv.end());
+  const size_t ib = 4 * iv.size(), db = 8 * std::max<size_t>(dv.size(), 1), fb = 4 * std::max<size_t>(fv.size(), 1);
+  HC_CUDA(h, dalloc(h, &ts.blob, ib + db + fb));
   HC_CUDA(h, cudaMemcpy(ts.blob, iv.data(), ib, cudaMemcpyHostToDevice));
   if (!dv.empty()) HC_CUDA(h, cudaMemcpy((char*)ts.blob + ib, dv.data(), 8 * dv.size(), cudaMemcpyHostToDevice));
+  if (!fv.empty()) HC_CUDA(h, cudaMemcpy((char*)ts.blob + ib + db, fv.data(), 4 * fv.size(), cudaMemcpyHostToDevice));
   const int* ibase = (const int*)ts.blob;
   const double* dbase = (const double*)((char*)ts.blob + ib);
+  const float* fbase = (const float*)((char*)ts.blob + ib + db);
   TypeDev& d = ts.dev;
   d.model = model;
   d.nv = c.nv;
@@ -1025,6 +1010,11 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
   d.edge_angle0 = dbase + o_ang;
   d.patch_d0 = dbase + o_pd;
   d.inner_l0 = dbase + o_il;
+  d.tri_a0f = fbase + o_a0;
+  d.edge_l0f = fbase + o_l0;
+  d.edge_angle0f = fbase + o_ang;
+  d.patch_d0f = fbase + o_pd;
+  d.inner_l0f = fbase + o_il;
   d.volume_eq = c.volume_eq;
   d.area_mean_eq = c.area_mean_eq;
   d.edge_mean_eq = c.edge_mean_eq;
@@ -1160,8 +1150,8 @@ int hc_read_populations(hc_handle* h, double* f) {
   if (!h || !f) return HC_ERR_INVALID;
   int rc;
   if ((rc = ensure_scratch(h, sizeof(double) * 19 * h->N)) != HC_OK) return rc;
-  if (h->f64) HC_CUDA(h, hcd::launch_convert_out<double>((const double*)h->f[h->cur], h->scratch, 19 * h->N, 1, h->N, h->stream));
-  else HC_CUDA(h, hcd::launch_convert_out<float>((const float*)h->f[h->cur], h->scratch, 19 * h->N, 1, h->N, h->stream));
+  if (h->f64) HC_CUDA(h, hcd::launch_stream_out<double>(lbm_view<double>(h, h->cur, h->cur), h->scratch, h->stream));
+  else HC_CUDA(h, hcd::launch_stream_out<float>(lbm_view<float>(h, h->cur, h->cur), h->scratch, h->stream));
   HC_CUDA(h, cudaMemcpyAsync(f, h->scratch, 8 * 19 * h->N, cudaMemcpyDeviceToHost, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
@@ -1172,8 +1162,8 @@ int hc_write_populations(hc_handle* h, const double* f) {
   int rc;
   if ((rc = ensure_scratch(h, sizeof(double) * 19 * h->N)) != HC_OK) return rc;
   HC_CUDA(h, cudaMemcpyAsync(h->scratch, f, 8 * 19 * h->N, cudaMemcpyHostToDevice, h->stream));
-  if (h->f64) HC_CUDA(h, hcd::launch_convert_in<double>(h->scratch, (double*)h->f[h->cur], 19 * h->N, 1.0, h->N, h->stream));
-  else HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)h->f[h->cur], 19 * h->N, 1.0, h->N, h->stream));
+  if (h->f64) HC_CUDA(h, hcd::launch_stream_in<double>(lbm_view<double>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
+  else HC_CUDA(h, hcd::launch_stream_in<float>(lbm_view<float>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
 }
@@ -1183,8 +1173,8 @@ int hc_read_force_field(hc_handle* h, double* F, int which) {
   int rc;
   if ((rc = ensure_scratch(h, sizeof(double) * 3 * h->N)) != HC_OK) return rc;
   const void* src = h->F[which ? 1 - h->cur : h->cur];
-  if (h->f64) HC_CUDA(h, hcd::launch_convert_out<double>((const double*)src, h->scratch, 3 * h->N, 0, h->N, h->stream));
-  else HC_CUDA(h, hcd::launch_convert_out<float>((const float*)src, h->scratch, 3 * h->N, 0, h->N, h->stream));
+  if (h->f64) HC_CUDA(h, hcd::launch_field_out<double>((const double*)src, h->scratch, h->N, h->stream));
+  else HC_CUDA(h, hcd::launch_field_out<float>((const float*)src, h->scratch, h->N, h->stream));
   HC_CUDA(h, cudaMemcpyAsync(F, h->scratch, 8 * 3 * h->N, cudaMemcpyDeviceToHost, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
@@ -1196,8 +1186,8 @@ int hc_write_force_field(hc_handle* h, const double* F) {
   if ((rc = ensure_scratch(h, sizeof(double) * 3 * h->N)) != HC_OK) return rc;
   HC_CUDA(h, cudaMemcpyAsync(h->scratch, F, 8 * 3 * h->N, cudaMemcpyHostToDevice, h->stream));
   for (int k = 0; k < 2; ++k) {
-    if (h->f64) HC_CUDA(h, hcd::launch_convert_in<double>(h->scratch, (double*)h->F[k], 3 * h->N, 0.0, h->N, h->stream));
-    else HC_CUDA(h, hcd::launch_convert_in<float>(h->scratch, (float*)h->F[k], 3 * h->N, 0.0, h->N, h->stream));
+    if (h->f64) HC_CUDA(h, hcd::launch_field_in<double>(h->scratch, (double*)h->F[k], h->N, h->stream));
+    else HC_CUDA(h, hcd::launch_field_in<float>(h->scratch, (float*)h->F[k], h->N, h->stream));
   }
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
@@ -1325,8 +1315,10 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
   if (!h || !in8) return HC_ERR_INVALID;
   if (in8[0] <= 0 || in8[1] <= 0 || in8[0] * in8[1] > 256 || in8[0] % 32 != 0)
     return fail(h, HC_ERR_INVALID, "collide-stream block must be a multiple of 32 wide and at most 256 threads");
-  for (int k = 2; k <= 4; ++k)
+  for (int k = 2; k <= 3; ++k)
     if (in8[k] <= 0 || in8[k] > 512 || in8[k] % 32 != 0) return fail(h, HC_ERR_INVALID, "bad block size");
+  if (in8[4] <= 0 || in8[4] > (h->f64 ? 512 : 1024) || in8[4] % 32 != 0)
+    return fail(h, HC_ERR_INVALID, "bad mechanics block size");
   std::memcpy(h->tune, in8, sizeof(h->tune));
   invalidate_graph(h);
   return HC_OK;

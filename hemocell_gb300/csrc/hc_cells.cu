@@ -1,209 +1,33 @@
-// CUDA kernels of the GB300 HemoCell IB-LBM step (sm_103a).
-//
-//  K1 collide_stream   D3Q19 Guo-forced BGK, push streaming with (moving)
-//                      bounce-back and periodic wrap; writes the next step's
-//                      force field (body force) so the reset is fused.
-//  K2 spread           IBM phi2 force spreading (FP atomics into F).
-//  K3+K5 interp_advance IBM velocity interpolation from the post-stream
-//                      populations, Euler advance, nearest-node binning and
-//                      wall deletion, one thread per vertex.
-//  K4 mechanics        RBC / PLT / WBC membrane forces, one CTA per cell,
-//                      vertex forces accumulated in shared memory.
-//  bin_csr             per-tile vertex lists sorted by (tile, cell, vertex).
-//
-// Templated on T = double (plain form) or float (mixed form).  Positions are
+// Cell kernels of the GB300 HemoCell step (sm_103a):
+//   K2 spread          IBM phi2 force spreading with FORCE_LIMIT clamp; one
+//                      vector atomic per node contribution (FP32); tags the
+//                      stencil nodes for the interpolation
+//   K3+K5 interp_advance  velocity interpolation from the tagged node
+//                      velocities, Euler advance, nearest-node bin, wall deletion
+//   K4 mechanics       RBC / PLT / WBC membrane forces, one CTA per cell
+//   binning            tile CSR sorted by (tile, cell, vertex)
+// Templated on T = double (plain form) or float (mixed form); positions are
 // double in both forms.
 #include <cmath>
 #include <cstdint>
 
-#include "hc_dev.h"
+#include "hc_d3q19.cuh"
 
 namespace hcd {
-
-// ---------------------------------------------------------------------------
-// D3Q19 velocity set: 0 rest, 1..9 one half, i+9 the opposite of i.
-__host__ __device__ constexpr int cxi(int i) {
-  return (i == 1 || i == 4 || i == 5 || i == 6 || i == 7) ? -1
-         : (i == 10 || i == 13 || i == 14 || i == 15 || i == 16) ? 1 : 0;
-}
-__host__ __device__ constexpr int cyi(int i) {
-  return (i == 2 || i == 4 || i == 8 || i == 9 || i == 14) ? -1
-         : (i == 5 || i == 11 || i == 13 || i == 17 || i == 18) ? 1 : 0;
-}
-__host__ __device__ constexpr int czi(int i) {
-  return (i == 3 || i == 6 || i == 8 || i == 16 || i == 18) ? -1
-         : (i == 7 || i == 9 || i == 12 || i == 15 || i == 17) ? 1 : 0;
-}
-__host__ __device__ constexpr int oppi(int i) { return i == 0 ? 0 : (i <= 9 ? i + 9 : i - 9); }
-__host__ __device__ constexpr double wi(int i) {
-  return i == 0 ? 1.0 / 3.0 : ((cxi(i) * cxi(i) + cyi(i) * cyi(i) + czi(i) * czi(i)) == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
-}
 
 template <typename T>
 __device__ __forceinline__ T tmax(T a, T b) {
   return a > b ? a : b;
 }
 
-// c . a for a lattice velocity c; the components are compile-time constants
-// once the direction loop is unrolled, so zero components cost nothing.
-template <typename T>
-__device__ __forceinline__ T cdot(int cx, int cy, int cz, T x, T y, T z) {
-  T r;
-  if (cx != 0) {
-    r = cx > 0 ? x : -x;
-    if (cy != 0) r = cy > 0 ? r + y : r - y;
-    if (cz != 0) r = cz > 0 ? r + z : r - z;
-  } else if (cy != 0) {
-    r = cy > 0 ? y : -y;
-    if (cz != 0) r = cz > 0 ? r + z : r - z;
-  } else {
-    r = cz > 0 ? z : (cz < 0 ? -z : T(0));
-  }
-  return r;
-}
-
-// ---------------------------------------------------------------------------
-// K1: collide + stream.  One thread per node; blocks are (bx, by) over x,y
-// and one z-plane per blockIdx.z.  The collision is written per opposite
-// pair (i, i+9) so the even and odd parts of equilibrium and Guo source are
-// shared: f*_{+c} = (1-w) f_{+c} + P + Q, f*_{-c} = (1-w) f_{-c} + P - Q.
-template <typename T>
-__global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
-  const int X = blockIdx.x * blockDim.x + threadIdx.x;
-  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Z = blockIdx.z;
-  if (X >= L.nx || Y >= L.ny) return;
-  const long long N = L.N;
-  const long long n = (long long)X + (long long)L.nx * ((long long)Y + (long long)L.ny * Z);
-  const uint32_t m = __ldg(L.nbmask + n);
-  if (m & NB_SOLID) return;
-
-  T f[19];
-#pragma unroll
-  for (int i = 0; i < 19; ++i) f[i] = L.fsrc[i * N + n];
-  const T Fx = L.Fcur[n], Fy = L.Fcur[N + n], Fz = L.Fcur[2 * N + n];
-
-  T d[10], p[10];
-#pragma unroll
-  for (int i = 1; i <= 9; ++i) {
-    d[i] = f[i + 9] - f[i];
-    p[i] = f[i + 9] + f[i];
-  }
-  const T rhoBar = f[0] + ((p[1] + p[2]) + (p[3] + p[4])) + ((p[5] + p[6]) + (p[7] + p[8])) + p[9];
-  const T jx = (d[1] + d[4]) + (d[5] + d[6]) + d[7];
-  const T jy = (d[2] + d[4]) - d[5] + (d[8] + d[9]);
-  const T jz = (d[3] + d[6]) - d[7] + (d[8] - d[9]);
-  const T rho = T(1) + rhoBar;
-  const T invRho = T(1) / rho;
-  const T ux = (jx + T(0.5) * Fx) * invRho;
-  const T uy = (jy + T(0.5) * Fy) * invRho;
-  const T uz = (jz + T(0.5) * Fz) * invRho;
-  const T uu = ux * ux + uy * uy + uz * uz;
-  const T uF = ux * Fx + uy * Fy + uz * Fz;
-  const T om = L.omega;
-  const T om1 = T(1) - om;
-  const T hs = T(1) - T(0.5) * om;
-  const T A = rhoBar - T(1.5) * rho * uu;  // even equilibrium part, without w
-  const T B = T(4.5) * rho;
-  const T K = T(3) * rho * om;
-  const T G = T(-3) * hs * uF;
-  const T H = T(9) * hs;
-  const T Lc = T(3) * hs;
-  // weight classes: axis w=1/18 and diagonal w=1/36
-  const T w1 = T(1.0 / 18.0);
-  const T Aw1 = om * w1 * A, Bw1 = om * w1 * B, Gw1 = w1 * G, Hw1 = w1 * H, Kw1 = w1 * K, Lw1 = w1 * Lc;
-  const T Aw2 = T(0.5) * Aw1, Bw2 = T(0.5) * Bw1, Gw2 = T(0.5) * Gw1, Hw2 = T(0.5) * Hw1, Kw2 = T(0.5) * Kw1,
-          Lw2 = T(0.5) * Lw1;
-
-  T post[19];
-  post[0] = om1 * f[0] + T(1.0 / 3.0) * (om * A + G);
-#pragma unroll
-  for (int i = 1; i <= 9; ++i) {
-    const int j = i + 9;  // positive direction c = c_j
-    const T cu = cdot(cxi(j), cyi(j), czi(j), ux, uy, uz);
-    const T cF = cdot(cxi(j), cyi(j), czi(j), Fx, Fy, Fz);
-    const bool axis = (wi(j) > 1.0 / 20.0);
-    const T Aw = axis ? Aw1 : Aw2, Bw = axis ? Bw1 : Bw2, Gw = axis ? Gw1 : Gw2;
-    const T Hw = axis ? Hw1 : Hw2, Kw = axis ? Kw1 : Kw2, Lw = axis ? Lw1 : Lw2;
-    const T P = (Bw * (cu * cu) + Aw) + (Hw * (cu * cF) + Gw);
-    const T Q = Kw * cu + Lw * cF;
-    post[j] = om1 * f[j] + (P + Q);
-    post[i] = om1 * f[i] + (P - Q);
-  }
-
-  // streaming (push) with bounce-back
-  const int xm = X == 0 ? L.nx - 1 : X - 1, xp = X == L.nx - 1 ? 0 : X + 1;
-  const int ym = Y == 0 ? L.ny - 1 : Y - 1, yp = Y == L.ny - 1 ? 0 : Y + 1;
-  const int zm = Z == 0 ? L.nz - 1 : Z - 1, zp = Z == L.nz - 1 ? 0 : Z + 1;
-  const uint32_t cls = m >> NB_CLASS_SHIFT;
-  L.fdst[n] = post[0];
-#pragma unroll
-  for (int i = 1; i < 19; ++i) {
-    const int ox = cxi(i) < 0 ? xm : (cxi(i) > 0 ? xp : X);
-    const int oy = cyi(i) < 0 ? ym : (cyi(i) > 0 ? yp : Y);
-    const int oz = czi(i) < 0 ? zm : (czi(i) > 0 ? zp : Z);
-    if (m & (1u << (i - 1))) {
-      uint32_t c = cls;
-      if (c == NB_CLASS_MIXED) {
-        const bool out = (!L.per[0] && ((cxi(i) < 0 && X == 0) || (cxi(i) > 0 && X == L.nx - 1))) ||
-                         (!L.per[1] && ((cyi(i) < 0 && Y == 0) || (cyi(i) > 0 && Y == L.ny - 1))) ||
-                         (!L.per[2] && ((czi(i) < 0 && Z == 0) || (czi(i) > 0 && Z == L.nz - 1)));
-        c = out ? 0u : (uint32_t)L.flag[(long long)ox + (long long)L.nx * ((long long)oy + (long long)L.ny * oz)];
-        if (c >= (uint32_t)MAX_WALL_CLASSES) c = 0;
-      }
-      const T cuw = T(cxi(i)) * L.uw[c][0] + T(cyi(i)) * L.uw[c][1] + T(czi(i)) * L.uw[c][2];
-      L.fdst[oppi(i) * N + n] = post[i] - T(6.0 * wi(i)) * cuw;
-    } else {
-      const long long o = (long long)ox + (long long)L.nx * ((long long)oy + (long long)L.ny * oz);
-      L.fdst[i * N + o] = post[i];
-    }
-  }
-  L.Fnext[n] = L.bodyz[Z];
-  L.Fnext[N + n] = L.bodyz[L.nz + Z];
-  L.Fnext[2 * N + n] = L.bodyz[2 * L.nz + Z];
-}
-
-template <typename T>
-cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s) {
-  if (bx <= 0) bx = 64;
-  if (by <= 0) by = 4;
-  dim3 block(bx, by, 1);
-  dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
-  k_collide_stream<T><<<grid, block, 0, s>>>(L);
-  return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// Node velocity of the post-stream populations with the collision force:
-// u = (sum_i c_i f_i + F/2) / rho   (Palabos computeVelocity for Guo forcing,
-// core/hemoCellParticleField.cpp:833).
-template <typename T>
-__device__ __forceinline__ void node_velocity(const T* __restrict__ f, const T* __restrict__ F, long long N,
-                                              long long n, T& ux, T& uy, T& uz) {
-  T d[10], p[10];
-  const T f0 = f[n];
-#pragma unroll
-  for (int i = 1; i <= 9; ++i) {
-    const T a = f[i * N + n], b = f[(i + 9) * N + n];
-    d[i] = b - a;
-    p[i] = b + a;
-  }
-  const T rhoBar = f0 + ((p[1] + p[2]) + (p[3] + p[4])) + ((p[5] + p[6]) + (p[7] + p[8])) + p[9];
-  const T jx = (d[1] + d[4]) + (d[5] + d[6]) + d[7];
-  const T jy = (d[2] + d[4]) - d[5] + (d[8] + d[9]);
-  const T jz = (d[3] + d[6]) - d[7] + (d[8] - d[9]);
-  const T rho = T(1) + rhoBar;
-  ux = (jx + T(0.5) * F[n]) / rho;
-  uy = (jy + T(0.5) * F[N + n]) / rho;
-  uz = (jz + T(0.5) * F[2 * N + n]) / rho;
-}
-
 // IBM phi2 kernel (core/immersedBoundaryMethod.h:37-41, :62-138).  The
 // reference scans the 3x3x3 nodes around floor(p+0.5) and keeps the nonzero
 // weights; phi2 vanishes beyond distance 1, so the kept nodes always lie in
-// the 2x2x2 block {floor(p), floor(p)+1}^3, which is scanned here in the same
+// the 2x2x2 block {floor(p), floor(p)+1}^3, scanned here in the same
 // (x, y, z) order.  Nodes off a non-periodic axis, zero weights and boundary
 // nodes are skipped (slot node = -1); the weights are renormalised to one.
+// FP64 evaluates phi2(p - q) exactly as the reference; FP32 takes the
+// fractional part once in double and the rest in float.
 template <typename T>
 struct Kern {
   long long node[8];
@@ -212,6 +36,7 @@ struct Kern {
 
 template <typename T>
 __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, double py, double pz, Kern<T>& K) {
+  constexpr bool kF64 = sizeof(T) == 8;
   const double P[3] = {px, py, pz};
   const int dims[3] = {L.nx, L.ny, L.nz};
   T phi[3][2];
@@ -219,22 +44,28 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     const double q0 = floor(P[a]);
+    if (kF64) {
+      phi[a][0] = tmax(T(1) - T(fabs(P[a] - q0)), T(0));
+      phi[a][1] = tmax(T(1) - T(fabs(P[a] - (q0 + 1.0))), T(0));
+    } else {
+      const T fr = (T)(P[a] - q0);  // in [0, 1)
+      phi[a][0] = T(1) - fr;
+      phi[a][1] = fr;
+    }
+    const long long qi = (long long)q0;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-      const double q = q0 + k;
-      const double r = P[a] - q;
-      phi[a][k] = tmax(T(1) - T(fabs(r)), T(0));
-      long long qi = (long long)q;
+      const long long q = qi + k;
       int wrapped;
-      if (qi < 0 || qi >= dims[a]) {
+      if (q < 0 || q >= dims[a]) {
         if (L.per[a]) {
-          long long mm = qi % dims[a];
+          long long mm = q % dims[a];
           wrapped = (int)(mm < 0 ? mm + dims[a] : mm);
         } else {
           wrapped = -1;
         }
       } else {
-        wrapped = (int)qi;
+        wrapped = (int)q;
       }
       idx[a][k] = wrapped;
     }
@@ -264,77 +95,49 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
 
 // ---------------------------------------------------------------------------
 // K2: spreadParticleForce (core/hemoCellParticleField.cpp:841-863) with the
-// FORCE_LIMIT clamp written back (:847-852).  The contributions of a CTA's
-// vertices are first summed per node in a shared-memory hash table (open
-// addressing, at most half full), then each distinct node gets one global
-// atomic per component.  The stencil nodes are tagged with the step stamp
-// so the interpolation computes node velocities only where needed.
-constexpr int SPREAD_BS = 128;
-constexpr int SPREAD_HASH = 2048;  // >= 2 * 8 * SPREAD_BS
-
+// FORCE_LIMIT clamp written back (:847-852); the stencil nodes are tagged
+// with the step stamp so the interpolation evaluates only those nodes.
 template <typename T>
-__global__ void __launch_bounds__(SPREAD_BS) k_spread(const LbmView<T> L, const VertexView<T> vv, const T f_limit) {
-  extern __shared__ double spread_smem[];
-  int* hkey = reinterpret_cast<int*>(spread_smem);
-  T* hval = reinterpret_cast<T*>(hkey + SPREAD_HASH);  // [3][SPREAD_HASH]
-  for (int k = threadIdx.x; k < SPREAD_HASH; k += blockDim.x) {
-    hkey[k] = -1;
-    hval[k] = T(0);
-    hval[SPREAD_HASH + k] = T(0);
-    hval[2 * SPREAD_HASH + k] = T(0);
-  }
-  __syncthreads();
+__global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const VertexView<T> vv, const T f_limit) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= vv.nvert || !vv.alive[vv.vcell[i]]) return;
   const uint32_t stamp = *L.stamp;
-  if (i < vv.nvert && vv.alive[vv.vcell[i]]) {
-    const long long V = vv.V;
-    T fx = vv.f[i], fy = vv.f[V + i], fz = vv.f[2 * V + i];
-    T mag = fx * fx;
-    mag += fy * fy;
-    mag += fz * fz;
-    mag = sqrt(mag);
-    if (mag > f_limit) {
-      const T s = f_limit / mag;
-      fx *= s;
-      fy *= s;
-      fz *= s;
-      vv.f[i] = fx;
-      vv.f[V + i] = fy;
-      vv.f[2 * V + i] = fz;
-    }
-    Kern<T> K;
-    ibm_weights(L, vv.x[i], vv.x[V + i], vv.x[2 * V + i], K);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      if (K.node[j] < 0) continue;
-      const int node = (int)K.node[j];
-      L.ntag[node] = stamp;
-      unsigned h = ((unsigned)node * 2654435761u) & (SPREAD_HASH - 1);
-      for (int probe = 0; probe < SPREAD_HASH; ++probe) {
-        const int old = atomicCAS(hkey + h, -1, node);
-        if (old == -1 || old == node) {
-          atomicAdd(hval + h, fx * K.w[j]);
-          atomicAdd(hval + SPREAD_HASH + h, fy * K.w[j]);
-          atomicAdd(hval + 2 * SPREAD_HASH + h, fz * K.w[j]);
-          break;
-        }
-        h = (h + 1) & (SPREAD_HASH - 1);
-      }
-    }
+  const long long V = vv.V;
+  T fx = vv.f[i], fy = vv.f[V + i], fz = vv.f[2 * V + i];
+  T mag = fx * fx;
+  mag += fy * fy;
+  mag += fz * fz;
+  mag = sqrt(mag);
+  if (mag > f_limit) {
+    const T s = f_limit / mag;
+    fx *= s;
+    fy *= s;
+    fz *= s;
+    vv.f[i] = fx;
+    vv.f[V + i] = fy;
+    vv.f[2 * V + i] = fz;
   }
-  __syncthreads();
+  Kern<T> K;
+  ibm_weights(L, vv.x[i], vv.x[V + i], vv.x[2 * V + i], K);
   T* F = const_cast<T*>(L.Fcur);
-  for (int k = threadIdx.x; k < SPREAD_HASH; k += blockDim.x) {
-    const int node = hkey[k];
-    if (node < 0) continue;
-    atomicAdd(F + node, hval[k]);
-    atomicAdd(F + L.N + node, hval[SPREAD_HASH + k]);
-    atomicAdd(F + 2 * L.N + node, hval[2 * SPREAD_HASH + k]);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (K.node[j] < 0) continue;
+    L.ntag[K.node[j]] = stamp;
+    FieldLayout<T>::add(F, L.N, K.node[j], fx * K.w[j], fy * K.w[j], fz * K.w[j]);
   }
 }
 
-// Tag the stencil nodes of every vertex (used when the interpolation runs
-// as a stage of its own, without the spread of the same step).
+template <typename T>
+cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs, cudaStream_t s) {
+  if (vv.nvert <= 0) return cudaSuccess;
+  if (bs <= 0) bs = 128;
+  k_spread<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, (T)f_limit);
+  return cudaGetLastError();
+}
+
+// Tag the stencil nodes of every vertex (the interpolation run as a stage
+// of its own, without the spread of the same step).
 template <typename T>
 __global__ void k_mark_nodes(const LbmView<T> L, const VertexView<T> vv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -350,25 +153,6 @@ template <typename T>
 cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s) {
   if (vv.nvert <= 0) return cudaSuccess;
   k_mark_nodes<T><<<(vv.nvert + 255) / 256, 256, 0, s>>>(L, vv);
-  return cudaGetLastError();
-}
-
-// Velocity of every tagged node from the post-stream populations (L.fsrc)
-// and the force of the collision that produced them (L.Fcur).
-template <typename T>
-__global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= L.N) return;
-  if (L.ntag[n] != *L.stamp) return;
-  T ux, uy, uz;
-  node_velocity(L.fsrc, L.Fcur, L.N, n, ux, uy, uz);
-  L.unode[n] = ux;
-  L.unode[L.N + n] = uy;
-  L.unode[2 * L.N + n] = uz;
-}
-template <typename T>
-cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s) {
-  k_node_velocity<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -392,31 +176,17 @@ cudaError_t launch_add_vertex_forces(const VertexView<T>& vv, const int* ids, co
   return cudaGetLastError();
 }
 
-template <typename T>
-cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs, cudaStream_t s) {
-  if (vv.nvert <= 0) return cudaSuccess;
-  (void)bs;
-  const size_t smem = SPREAD_HASH * (sizeof(int) + 3 * sizeof(T));
-  k_spread<T><<<(vv.nvert + SPREAD_BS - 1) / SPREAD_BS, SPREAD_BS, smem, s>>>(L, vv, (T)f_limit);
-  return cudaGetLastError();
-}
-
-template <typename T>
-cudaError_t prepare_spread() {
-  return cudaFuncSetAttribute(k_spread<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(SPREAD_HASH * (sizeof(int) + 3 * sizeof(T))));
-}
-
 // ---------------------------------------------------------------------------
-// K3+K5: interpolateFluidVelocity (core/hemoCellParticleField.cpp:819-839),
-// advanceParticles (:566-588, core/hemoCellParticle.h:188-203) and the
-// per-vertex bin of update_pg (:137-168).  L.fsrc holds the post-stream
-// populations, L.Fcur the force of the collision that produced them.
+// K3+K5: interpolateFluidVelocity (core/hemoCellParticleField.cpp:819-839)
+// from the node velocities of this step (L.unode), advanceParticles
+// (:566-588, core/hemoCellParticle.h:188-203) and the per-vertex bin of
+// update_pg (:137-168).  Thread 0 advances the device step stamp; no thread
+// of this kernel reads it.
 template <typename T>
 __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, const VertexView<T> vv, const TileGrid tg,
                                                         const int do_interp, const int do_advance) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) *L.stamp += 1;  // the next spread tags with a fresh stamp; nothing here reads it
+  if (i == 0) *L.stamp += 1;
   if (i >= vv.nvert) return;
   const int cell = vv.vcell[i];
   if (!vv.alive[cell]) {
@@ -436,14 +206,16 @@ __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, cons
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       if (K.node[j] < 0) continue;
-      vx += L.unode[K.node[j]] * K.w[j];
-      vy += L.unode[L.N + K.node[j]] * K.w[j];
-      vz += L.unode[2 * L.N + K.node[j]] * K.w[j];
+      T ux, uy, uz;
+      FieldLayout<T>::load(L.unode, L.N, K.node[j], ux, uy, uz);
+      vx += ux * K.w[j];
+      vy += uy * K.w[j];
+      vz += uz * K.w[j];
     }
     vv.v[i] = vx;
     vv.v[V + i] = vy;
     vv.v[2 * V + i] = vz;
-    if (!(isfinite((double)vx) && isfinite((double)vy) && isfinite((double)vz))) atomicOr(vv.status, 1u);
+    if (!(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(vv.status, 1u);
   } else {
     vx = vv.v[i];
     vy = vv.v[V + i];
@@ -457,7 +229,6 @@ __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, cons
     vv.x[V + i] = py;
     vv.x[2 * V + i] = pz;
   }
-  // nearest node and tile
   const double P[3] = {px, py, pz};
   const int dims[3] = {L.nx, L.ny, L.nz};
   int q[3];
@@ -492,9 +263,9 @@ __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, cons
 template <typename T>
 cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, int do_interp,
                                   int do_advance, int bs, cudaStream_t s) {
-  if (vv.nvert <= 0) return cudaSuccess;
   if (bs <= 0) bs = 128;
-  k_interp_advance<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, tg, do_interp, do_advance);
+  const int n = vv.nvert > 0 ? vv.nvert : 1;  // one thread at least: it advances the stamp
+  k_interp_advance<T><<<(n + bs - 1) / bs, bs, 0, s>>>(L, vv, tg, do_interp, do_advance);
   return cudaGetLastError();
 }
 
@@ -570,15 +341,32 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
 }
 
 template <typename T>
+__device__ __forceinline__ T rest_value(const double* d, const float* f, int k);
+template <>
+__device__ __forceinline__ double rest_value<double>(const double* d, const float*, int k) {
+  return d[k];
+}
+template <>
+__device__ __forceinline__ float rest_value<float>(const double*, const float* f, int k) {
+  return f[k];
+}
+
+template <typename T>
 size_t mechanics_smem_bytes(int nv) {
   return 34 * sizeof(double) + 6 * (size_t)nv * sizeof(T);
 }
 
+// One CTA per cell (grid-stride over the cell list).  Pass A runs the faces
+// (volume terms, area force); after the block reduction of the volume, pass B
+// runs the volume force of every face, the bending of every vertex (RBC,
+// WBC), every edge (link, membrane viscosity, platelet dihedral bending) and
+// every inner link as one merged item loop.  Forces accumulate in shared
+// memory and are written once.
 template <typename T>
-__global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) k_mechanics(const MechView<T> M) {
   extern __shared__ double smem_d[];
   __shared__ TypeDev tshared;
-  double* red = smem_d;                  // 34 doubles
+  double* red = smem_d;  // 34 doubles
   T* sx = reinterpret_cast<T*>(smem_d + 34);
   const VertexView<T>& vv = M.vv;
   const long long V = vv.V;
@@ -594,7 +382,7 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
     const int voff = M.cell_voff[cell];
     T* sf = sx + 3 * nv;
     const bool alive = vv.alive[cell] != 0;
-    // positions: absolute in FP64, relative to vertex 0 in FP32
+    // positions: absolute in FP64 (as the reference), relative to vertex 0 in FP32
     const double r0x = kF64 ? 0.0 : vv.x[voff], r0y = kF64 ? 0.0 : vv.x[V + voff],
                  r0z = kF64 ? 0.0 : vv.x[2 * V + voff];
     for (int k = tid; k < nv; k += bs) {
@@ -607,7 +395,7 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
     }
     __syncthreads();
     if (alive) {
-      // --- faces: volume, area force (rbcHighOrderModel.cpp:56-98)
+      // --- pass A: faces, volume terms and area force (rbcHighOrderModel.cpp:56-98)
       double vol = 0.0;
       for (int k = tid; k < t.nf; k += bs) {
         const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
@@ -619,7 +407,7 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
           const double v102 = (double)v1.x * v0.y * v2.z, v012 = (double)v0.x * v1.y * v2.z;
           vol += (-v210 + v120 + v201 - v021 - v102 + v012);
         } else {
-          // v0 . ((v1-v0) x (v2-v0)) == v0 . (v1 x v2); FP32 term, FP64 sum
+          // v0 . ((v1-v0) x (v2-v0)) == v0 . (v1 x v2): FP32 term, FP64 sum
           vol += (double)vdot(v0, n);
         }
         const T nn = vnorm(n);
@@ -630,7 +418,7 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
         } else {
           area = T(0);
         }
-        const T a0 = (T)t.tri_a0[k];
+        const T a0 = rest_value<T>(t.tri_a0, t.tri_a0f, k);
         const T ar = (area - a0) / a0;
         const T afm = (T)t.k_area * (ar + ar / fabs(T(kMaxArea) - ar * ar));
         const V3t<T> cen = {(v0.x + v1.x + v2.x) / T(3), (v0.y + v1.y + v2.y) / T(3), (v0.z + v1.z + v2.z) / T(3)};
@@ -639,36 +427,38 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
         add3(sf, i2, vscale(cen - v2, afm));
       }
       const double volume = block_sum<T>(vol, red) * (1.0 / 6.0);
+      // volume constraint in FP64 (rbcHighOrderModel.cpp:100-104)
       const double vfr = (volume - t.volume_eq) / t.volume_eq;
       const double vforce = -t.k_volume * vfr / fabs(kMaxVol - vfr * vfr);
-      const double vforce_per_area = vforce / t.area_mean_eq;
-      // --- faces: volume force (:103-124)
-      for (int k = tid; k < t.nf; k += bs) {
-        const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
-        const V3t<T> v0 = ld3(sx, i0), v1 = ld3(sx, i1), v2 = ld3(sx, i2);
-        V3t<T> n = vcross(v1 - v0, v2 - v0);
-        const T nn = vnorm(n);
-        T area;
-        if (nn != T(0)) {
-          area = T(0.5) * nn;
-          n = {n.x / nn, n.y / nn, n.z / nn};
-        } else {
-          area = T(0);
-          n = {T(0), T(0), T(0)};
-        }
-        V3t<T> lvf;
-        if (kF64) {
-          lvf = vscale(vscale(n, (T)vforce), area / (T)t.area_mean_eq);
-        } else {
-          lvf = vscale(n, (T)(vforce_per_area * (double)area));
-        }
-        add3(sf, i0, lvf);
-        add3(sf, i1, lvf);
-        add3(sf, i2, lvf);
-      }
-      // --- vertices: bending (rbcHighOrderModel.cpp:127-166), RBC and WBC
-      if (t.model != 1) {
-        for (int i = tid; i < nv; i += bs) {
+      const T vforce_per_area = (T)(vforce / t.area_mean_eq);
+      const bool visc = (t.model != 0) || (t.eta_m != 0.0);
+      const int nb = (t.model != 1) ? nv : 0;
+      const int e0 = t.nf + nb, e1 = e0 + t.ne, total = e1 + t.ni;
+      // --- pass B: volume force, bending, edges, inner links
+      for (int k = tid; k < total; k += bs) {
+        if (k < t.nf) {
+          // volume force per face (rbcHighOrderModel.cpp:103-124)
+          const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
+          const V3t<T> v0 = ld3(sx, i0), v1 = ld3(sx, i1), v2 = ld3(sx, i2);
+          V3t<T> n = vcross(v1 - v0, v2 - v0);
+          const T nn = vnorm(n);
+          T area;
+          if (nn != T(0)) {
+            area = T(0.5) * nn;
+            n = {n.x / nn, n.y / nn, n.z / nn};
+          } else {
+            area = T(0);
+            n = {T(0), T(0), T(0)};
+          }
+          V3t<T> lvf;
+          if (kF64) lvf = vscale(vscale(n, (T)vforce), area / (T)t.area_mean_eq);
+          else lvf = vscale(n, vforce_per_area * area);
+          add3(sf, i0, lvf);
+          add3(sf, i1, lvf);
+          add3(sf, i2, lvf);
+        } else if (k < e0) {
+          // bending per vertex (rbcHighOrderModel.cpp:127-166)
+          const int i = k - t.nf;
           const int rn = t.ring_n[i];
           const int* rg = t.ring + 6 * i;
           const V3t<T> xi = ld3(sx, i);
@@ -689,75 +479,74 @@ __global__ void __launch_bounds__(512) k_mechanics(const MechView<T> M) {
           const T pl = vnorm(pn);
           pn = {pn.x / pl, pn.y / pl, pn.z / pl};
           const T ndev = vdot(pn, dev);
-          const T dDev = (ndev - (T)t.patch_d0[i]) / (T)t.edge_mean_eq;
+          const T dDev = (ndev - rest_value<T>(t.patch_d0, t.patch_d0f, i)) / (T)t.edge_mean_eq;
           const V3t<T> bf = vscale(pn, (T)t.k_bend * (dDev + dDev / fabs(T(kMaxBend) - dDev * dDev)));
           add3(sf, i, bf);
           const V3t<T> nbf = {-bf.x / (T)rn, -bf.y / (T)rn, -bf.z / (T)rn};
           for (int j = 0; j < rn; ++j) add3(sf, rg[j], nbf);
-        }
-      }
-      // --- edges: link, membrane viscosity, platelet dihedral bending
-      const bool visc = (t.model != 0) || (t.eta_m != 0.0);
-      for (int e = tid; e < t.ne; e += bs) {
-        const int a = t.edges[2 * e], b = t.edges[2 * e + 1];
-        const V3t<T> p0 = ld3(sx, a), p1 = ld3(sx, b);
-        const V3t<T> ev = p1 - p0;
-        const T L = vnorm(ev);
-        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
-        const T l0 = (T)t.edge_l0[e];
-        const T ef = (L - l0) / l0;
-        const T fs = (T)t.k_link * (ef + ef / fabs(T(kMaxLink) - ef * ef));
-        const V3t<T> force = vscale(uv, fs);
-        V3t<T> fa = force, fb = {-force.x, -force.y, -force.z};
-        if (visc) {
-          const V3t<T> va = {vv.v[voff + a], vv.v[V + voff + a], vv.v[2 * V + voff + a]};
-          const V3t<T> vb = {vv.v[voff + b], vv.v[V + voff + b], vv.v[2 * V + voff + b]};
-          V3t<T> fv = vscale(vscale(uv, vdot(vb - va, uv)), (T)t.eta_m);
-          const T mm = vnorm(fv);
-          if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
-          fa = fa + fv;
-          fb = fb - fv;
-        }
-        if (t.model == 1) {
-          const int* A = t.tris + 3 * t.bend_tris[2 * e];
-          const int* B = t.tris + 3 * t.bend_tris[2 * e + 1];
-          const V3t<T> V1 = unit_normal(ld3(sx, A[0]), ld3(sx, A[1]), ld3(sx, A[2]));
-          const V3t<T> V2 = unit_normal(ld3(sx, B[0]), ld3(sx, B[1]), ld3(sx, B[2]));
-          const T angle = atan2(vdot(vcross(V1, V2), uv), vdot(V1, V2));
-          const T af = angle - (T)t.edge_angle0[e];
-          const T fm = (T)t.k_bend * (af + af / fabs(T(kMaxPltBend) - af * af));
-          const V3t<T> bfv = vscale(V1 + V2, fm * T(0.5));
-          fa = fa + bfv;
-          fb = fb + bfv;
-          const V3t<T> nb = {-bfv.x, -bfv.y, -bfv.z};
-          add3(sf, t.bend_outer[2 * e], nb);
-          add3(sf, t.bend_outer[2 * e + 1], nb);
-        }
-        add3(sf, a, fa);
-        add3(sf, b, fb);
-      }
-      // --- inner edges
-      for (int e = tid; e < t.ni; e += bs) {
-        const int a = t.inner[2 * e], b = t.inner[2 * e + 1];
-        const V3t<T> ev = ld3(sx, b) - ld3(sx, a);
-        const T L = vnorm(ev);
-        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
-        if (t.model == 1) {  // pltSimpleModel.cpp:188-205
-          const T l0 = (T)t.inner_l0[e];
+        } else if (k < e1) {
+          // link, membrane viscosity, platelet dihedral bending
+          const int e = k - e0;
+          const int a = t.edges[2 * e], b = t.edges[2 * e + 1];
+          const V3t<T> p0 = ld3(sx, a), p1 = ld3(sx, b);
+          const V3t<T> ev = p1 - p0;
+          const T L = vnorm(ev);
+          const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
+          const T l0 = rest_value<T>(t.edge_l0, t.edge_l0f, e);
           const T ef = (L - l0) / l0;
-          const V3t<T> force = vscale(uv, (T)t.k_link * T(5) * ef);
-          add3(sf, a, force);
-          add3(sf, b, V3t<T>{-force.x, -force.y, -force.z});
-        } else if (t.model == 2) {  // wbcHighOrderModel.cpp:202-223
-          if (L < T(2) * (T)t.radius) {
-            const V3t<T> force = vscale(vscale(uv, T(1) - L / (T(2) * (T)t.radius)), (T)t.k_cyto);
-            add3(sf, a, V3t<T>{-force.x, -force.y, -force.z});
-            add3(sf, b, force);
+          const T fs = (T)t.k_link * (ef + ef / fabs(T(kMaxLink) - ef * ef));
+          const V3t<T> force = vscale(uv, fs);
+          V3t<T> fa = force, fb = {-force.x, -force.y, -force.z};
+          if (visc) {
+            const V3t<T> va = {vv.v[voff + a], vv.v[V + voff + a], vv.v[2 * V + voff + a]};
+            const V3t<T> vb = {vv.v[voff + b], vv.v[V + voff + b], vv.v[2 * V + voff + b]};
+            V3t<T> fv = vscale(vscale(uv, vdot(vb - va, uv)), (T)t.eta_m);
+            const T mm = vnorm(fv);
+            if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
+            fa = fa + fv;
+            fb = fb - fv;
           }
-          if (L < T(2) * (T)t.core_radius) {
-            const V3t<T> force = vscale(vscale(uv, T(1) - L / (T(2) * (T)t.core_radius)), (T)t.k_inner_rigid);
-            add3(sf, a, V3t<T>{-force.x, -force.y, -force.z});
-            add3(sf, b, force);
+          if (t.model == 1) {  // pltSimpleModel.cpp:156-182
+            const int* A = t.tris + 3 * t.bend_tris[2 * e];
+            const int* B = t.tris + 3 * t.bend_tris[2 * e + 1];
+            const V3t<T> V1 = unit_normal(ld3(sx, A[0]), ld3(sx, A[1]), ld3(sx, A[2]));
+            const V3t<T> V2 = unit_normal(ld3(sx, B[0]), ld3(sx, B[1]), ld3(sx, B[2]));
+            const T angle = atan2(vdot(vcross(V1, V2), uv), vdot(V1, V2));
+            const T af = angle - rest_value<T>(t.edge_angle0, t.edge_angle0f, e);
+            const T fm = (T)t.k_bend * (af + af / fabs(T(kMaxPltBend) - af * af));
+            const V3t<T> bfv = vscale(V1 + V2, fm * T(0.5));
+            fa = fa + bfv;
+            fb = fb + bfv;
+            const V3t<T> nbv = {-bfv.x, -bfv.y, -bfv.z};
+            add3(sf, t.bend_outer[2 * e], nbv);
+            add3(sf, t.bend_outer[2 * e + 1], nbv);
+          }
+          add3(sf, a, fa);
+          add3(sf, b, fb);
+        } else {
+          // inner links
+          const int e = k - e1;
+          const int a = t.inner[2 * e], b = t.inner[2 * e + 1];
+          const V3t<T> ev = ld3(sx, b) - ld3(sx, a);
+          const T L = vnorm(ev);
+          const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
+          if (t.model == 1) {  // pltSimpleModel.cpp:188-205
+            const T l0 = rest_value<T>(t.inner_l0, t.inner_l0f, e);
+            const T ef = (L - l0) / l0;
+            const V3t<T> force = vscale(uv, (T)t.k_link * T(5) * ef);
+            add3(sf, a, force);
+            add3(sf, b, V3t<T>{-force.x, -force.y, -force.z});
+          } else if (t.model == 2) {  // wbcHighOrderModel.cpp:202-223
+            if (L < T(2) * (T)t.radius) {
+              const V3t<T> force = vscale(vscale(uv, T(1) - L / (T(2) * (T)t.radius)), (T)t.k_cyto);
+              add3(sf, a, V3t<T>{-force.x, -force.y, -force.z});
+              add3(sf, b, force);
+            }
+            if (L < T(2) * (T)t.core_radius) {
+              const V3t<T> force = vscale(vscale(uv, T(1) - L / (T(2) * (T)t.core_radius)), (T)t.k_inner_rigid);
+              add3(sf, a, V3t<T>{-force.x, -force.y, -force.z});
+              add3(sf, b, force);
+            }
           }
         }
       }
@@ -782,66 +571,25 @@ template <typename T>
 cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s) {
   if (M.ncells <= 0) return cudaSuccess;
   if (bs <= 0) bs = 256;
+  if (bs > (sizeof(T) == 8 ? 512 : 1024)) bs = sizeof(T) == 8 ? 512 : 1024;
   if (grid <= 0 || grid > M.ncells) grid = M.ncells;
   k_mechanics<T><<<grid, bs, M.dyn_smem, s>>>(M);
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// Fluid readback: rho and u = (j + F/2)/rho of every node.
+// device [3][Vcap] (T) -> [V][3] double
 template <typename T>
-__global__ void k_moments(const LbmView<T> L, double* rho, double* u) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= L.N) return;
-  const long long N = L.N;
-  T rb = T(0);
-  for (int i = 0; i < 19; ++i) rb += L.fsrc[i * N + n];
-  T ux, uy, uz;
-  node_velocity(L.fsrc, L.Fcur, N, n, ux, uy, uz);
-  if (rho) rho[n] = 1.0 + (double)rb;
-  if (u) {
-    u[n] = ux;
-    u[N + n] = uy;
-    u[2 * N + n] = uz;
-  }
+__global__ void k_soa_to_aos(const T* src, double* dst, long long V, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[3 * (long long)i] = (double)src[i];
+  dst[3 * (long long)i + 1] = (double)src[V + i];
+  dst[3 * (long long)i + 2] = (double)src[2 * V + i];
 }
 template <typename T>
-cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s) {
-  k_moments<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L, rho, u);
-  return cudaGetLastError();
-}
-
-// population / field conversion between double host layout and T device layout
-template <typename T>
-__global__ void k_convert_in(const double* src, T* dst, long long n, double shift, long long N) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  double s = 0.0;
-  if (shift != 0.0) {
-    const int i = (int)(k / N);
-    s = i == 0 ? 1.0 / 3.0 : (((i - 1) % 9) < 3 ? 1.0 / 18.0 : 1.0 / 36.0);
-  }
-  dst[k] = (T)(src[k] - s);
-}
-template <typename T>
-__global__ void k_convert_out(const T* src, double* dst, long long n, int add_w, long long N) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  double s = 0.0;
-  if (add_w) {
-    const int i = (int)(k / N);
-    s = i == 0 ? 1.0 / 3.0 : (((i - 1) % 9) < 3 ? 1.0 / 18.0 : 1.0 / 36.0);
-  }
-  dst[k] = (double)src[k] + s;
-}
-template <typename T>
-cudaError_t launch_convert_in(const double* src, T* dst, long long n, double shift, long long N, cudaStream_t s) {
-  k_convert_in<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n, shift, N);
-  return cudaGetLastError();
-}
-template <typename T>
-cudaError_t launch_convert_out(const T* src, double* dst, long long n, int add_w, long long N, cudaStream_t s) {
-  k_convert_out<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n, add_w, N);
+cudaError_t launch_soa_to_aos(const T* src, double* dst, long long V, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_soa_to_aos<T><<<(n + 255) / 256, 256, 0, s>>>(src, dst, V, n);
   return cudaGetLastError();
 }
 
@@ -1036,13 +784,9 @@ cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, cons
   return cudaGetLastError();
 }
 
-// explicit instantiations
-#define HC_INST(T)                                                                                              \
-  template cudaError_t launch_collide_stream<T>(const LbmView<T>&, int, int, cudaStream_t);                    \
+#define HC_CELL_INST(T)                                                                                        \
   template cudaError_t launch_spread<T>(const LbmView<T>&, const VertexView<T>&, double, int, cudaStream_t);   \
-  template cudaError_t prepare_spread<T>();                                                                    \
   template cudaError_t launch_mark_nodes<T>(const LbmView<T>&, const VertexView<T>&, cudaStream_t);            \
-  template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                               \
   template cudaError_t launch_add_vertex_forces<T>(const VertexView<T>&, const int*, const double*, int,       \
                                                    cudaStream_t);                                              \
   template cudaError_t launch_interp_advance<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&, int, \
@@ -1050,12 +794,10 @@ cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, cons
   template cudaError_t launch_mechanics<T>(const MechView<T>&, int, int, cudaStream_t);                        \
   template size_t mechanics_smem_bytes<T>(int);                                                                \
   template cudaError_t prepare_mechanics<T>(int);                                                              \
-  template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);                   \
+  template cudaError_t launch_soa_to_aos<T>(const T*, double*, long long, int, cudaStream_t);                  \
   template cudaError_t launch_bin_vertices<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&,         \
-                                              cudaStream_t);                                                   \
-  template cudaError_t launch_convert_in<T>(const double*, T*, long long, double, long long, cudaStream_t);     \
-  template cudaError_t launch_convert_out<T>(const T*, double*, long long, int, long long, cudaStream_t);
-HC_INST(double)
-HC_INST(float)
+                                              cudaStream_t);
+HC_CELL_INST(double)
+HC_CELL_INST(float)
 
 }  // namespace hcd

@@ -1,8 +1,10 @@
-// Device-side views shared by the kernels (hc_kernels.cu) and the C ABI
-// (hc_api.cu).  All arrays are structure-of-arrays in HBM:
-//   populations f[19][N] stored as f_i - w_i (T = double or float)
-//   force field F[3][N] (T), double-buffered: the force of the collision in
-//   flight and the next step's force (body force + spreading)
+// Device-side views shared by the kernels (hc_lattice.cu, hc_cells.cu) and
+// the C ABI (hc_api.cu).  Arrays in HBM:
+//   populations f[19][N]: post-collision values f*_i - w_i of the last
+//   collision (T = double or float); readers pull the post-stream values
+//   force field, double-buffered (the force of the collision in flight and
+//   the next step's force = body force + spreading): float4 per node in
+//   FP32, [3][N] in FP64
 //   vertex x[3][V] (always double), v[3][V] and force[3][V] (T)
 #pragma once
 #include <cuda_runtime.h>
@@ -50,6 +52,11 @@ struct TypeDev {
   const double* edge_angle0;
   const double* patch_d0;
   const double* inner_l0;
+  const float* tri_a0f;  // FP32 copies for the mixed form
+  const float* edge_l0f;
+  const float* edge_angle0f;
+  const float* patch_d0f;
+  const float* inner_l0f;
   double volume_eq, area_mean_eq, edge_mean_eq;
   double k_link, k_bend, k_volume, k_area, eta_m, k_inner_rigid, k_cyto, core_radius, radius;
 };
@@ -84,15 +91,33 @@ struct MechView {
   int dyn_smem;       // bytes available per CTA
 };
 
-// Launch wrappers (hc_kernels.cu); each enqueues on `s` and returns the
-// launch error code.
+// Launch wrappers; each enqueues on `s` and returns the launch error code.
+// hc_lattice.cu
 template <typename T>
 cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s);
 template <typename T>
-cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs,
-                          cudaStream_t s);
+cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s);
 template <typename T>
-cudaError_t prepare_spread();
+cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s);
+template <typename T>
+cudaError_t launch_stream_out(const LbmView<T>& L, double* out, cudaStream_t s);
+template <typename T>
+cudaError_t launch_stream_in(const LbmView<T>& L, const double* in, double rho, const double* u3, cudaStream_t s);
+template <typename T>
+cudaError_t launch_field_out(const T* F, double* out, long long N, cudaStream_t s);
+template <typename T>
+cudaError_t launch_field_in(const double* in, T* F, long long N, cudaStream_t s);
+template <typename T>
+cudaError_t launch_fill_body(T* F, const T* bodyz, long long plane, int nz, long long N, cudaStream_t s);
+template <typename T>
+size_t field_bytes(long long N);
+template <typename T>
+cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream_t s);
+// hc_cells.cu
+template <typename T>
+cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s);
 template <typename T>
 cudaError_t launch_add_vertex_forces(const VertexView<T>& vv, const int* ids, const double* fext, int n,
                                      cudaStream_t s);
@@ -100,23 +125,13 @@ template <typename T>
 cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg,
                                   int do_interp, int do_advance, int bs, cudaStream_t s);
 template <typename T>
-cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s);
-template <typename T>
-cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s);
-template <typename T>
 cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s);
 template <typename T>
 size_t mechanics_smem_bytes(int nv);
 template <typename T>
 cudaError_t prepare_mechanics(int smem_bytes);
 template <typename T>
-cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s);
-template <typename T>
-cudaError_t launch_convert_in(const double* src, T* dst, long long n, double shift_by_weight, long long N,
-                              cudaStream_t s);
-template <typename T>
-cudaError_t launch_convert_out(const T* src, double* dst, long long n, int add_weight, long long N,
-                               cudaStream_t s);
+cudaError_t launch_soa_to_aos(const T* src, double* dst, long long V, int n, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bin_vertices(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, cudaStream_t s);
 // binning: tile CSR sorted by (tile, cell, vertex)

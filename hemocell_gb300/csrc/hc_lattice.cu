@@ -1,0 +1,294 @@
+// Lattice kernels of the GB300 HemoCell step (sm_103a):
+//   K1 collide_stream  pull + D3Q19 Guo-forced BGK collision, aligned writes
+//                      of the post-collision state; writes the next step's
+//                      force field (body force), fusing the force reset.
+//   node_velocity      post-stream velocity of the nodes the IBM stencils touch
+//   moments / stream_out / stream_in / field conversions for readback and set-up
+#include <cmath>
+#include <cstdint>
+
+#include "hc_d3q19.cuh"
+
+namespace hcd {
+
+// ---------------------------------------------------------------------------
+// K1.  One thread per node; blocks (bx, by) over x,y and one z-plane per
+// blockIdx.z.  The collision is written per opposite pair (i, i+9), sharing
+// the even and odd parts of equilibrium and Guo source:
+//   f*_{+c} = (1-w) f_{+c} + P + Q,   f*_{-c} = (1-w) f_{-c} + P - Q
+// with rho u = sum c f + F/2 (Guo, Zheng & Shi 2002).
+template <typename T>
+__global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = blockIdx.z;
+  if (X >= L.nx || Y >= L.ny) return;
+  const long long N = L.N;
+  const long long n = (long long)X + (long long)L.nx * ((long long)Y + (long long)L.ny * Z);
+  const uint32_t m = __ldg(L.nbmask + n);
+  if (m & NB_SOLID) return;
+
+  T f[19];
+  pull(L, L.fsrc, X, Y, Z, n, m, f);
+  T Fx, Fy, Fz;
+  FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
+
+  T rhoBar, jx, jy, jz;
+  moments(f, rhoBar, jx, jy, jz);
+  const T rho = T(1) + rhoBar;
+  const T invRho = T(1) / rho;
+  const T ux = (jx + T(0.5) * Fx) * invRho;
+  const T uy = (jy + T(0.5) * Fy) * invRho;
+  const T uz = (jz + T(0.5) * Fz) * invRho;
+  const T uu = ux * ux + uy * uy + uz * uz;
+  const T uF = ux * Fx + uy * Fy + uz * Fz;
+  const T om = L.omega;
+  const T om1 = T(1) - om;
+  const T hs = T(1) - T(0.5) * om;
+  const T A = rhoBar - T(1.5) * rho * uu;  // even equilibrium part without w
+  const T B = T(4.5) * rho;
+  const T K = T(3) * rho * om;
+  const T G = T(-3) * hs * uF;
+  const T H = T(9) * hs;
+  const T Lc = T(3) * hs;
+  const T w1 = T(1.0 / 18.0);
+  const T Aw1 = om * w1 * A, Bw1 = om * w1 * B, Gw1 = w1 * G, Hw1 = w1 * H, Kw1 = w1 * K, Lw1 = w1 * Lc;
+  const T Aw2 = T(0.5) * Aw1, Bw2 = T(0.5) * Bw1, Gw2 = T(0.5) * Gw1, Hw2 = T(0.5) * Hw1, Kw2 = T(0.5) * Kw1,
+          Lw2 = T(0.5) * Lw1;
+
+  L.fdst[n] = om1 * f[0] + T(1.0 / 3.0) * (om * A + G);
+#pragma unroll
+  for (int i = 1; i <= 9; ++i) {
+    const int j = i + 9;  // c = c_j
+    const T cu = cdot(cxi(j), cyi(j), czi(j), ux, uy, uz);
+    const T cF = cdot(cxi(j), cyi(j), czi(j), Fx, Fy, Fz);
+    const bool axis = (wi(j) > 1.0 / 20.0);
+    const T Aw = axis ? Aw1 : Aw2, Bw = axis ? Bw1 : Bw2, Gw = axis ? Gw1 : Gw2;
+    const T Hw = axis ? Hw1 : Hw2, Kw = axis ? Kw1 : Kw2, Lw = axis ? Lw1 : Lw2;
+    const T P = (Bw * (cu * cu) + Aw) + (Hw * (cu * cF) + Gw);
+    const T Q = Kw * cu + Lw * cF;
+    L.fdst[j * N + n] = om1 * f[j] + (P + Q);
+    L.fdst[i * N + n] = om1 * f[i] + (P - Q);
+  }
+  FieldLayout<T>::store(L.Fnext, N, n, L.bodyz[Z], L.bodyz[L.nz + Z], L.bodyz[2 * L.nz + Z]);
+}
+
+template <typename T>
+cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s) {
+  if (bx <= 0) bx = 64;
+  if (by <= 0) by = 4;
+  dim3 block(bx, by, 1);
+  dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
+  k_collide_stream<T><<<grid, block, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Velocity u = (sum c f + F/2)/rho of the post-stream state at every node
+// tagged by this step's stencils (Palabos computeVelocity for Guo forcing,
+// core/hemoCellParticleField.cpp:833); L.fsrc is the post-collision state,
+// L.Fcur the force of that collision.
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L.N) return;
+  if (L.ntag[n] != *L.stamp) return;
+  const uint32_t m = L.nbmask[n];
+  int X, Y, Z;
+  node_xyz(n, L.nx, L.ny, X, Y, Z);
+  T f[19];
+  pull(L, L.fsrc, X, Y, Z, n, m, f);
+  T rhoBar, jx, jy, jz, Fx, Fy, Fz;
+  moments(f, rhoBar, jx, jy, jz);
+  FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
+  const T rho = T(1) + rhoBar;
+  FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
+                        (jz + T(0.5) * Fz) / rho);
+}
+template <typename T>
+cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s) {
+  k_node_velocity<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+// Fluid readback: rho and u of every node (post-stream, force of the last collision).
+template <typename T>
+__global__ void k_moments(const LbmView<T> L, double* rho, double* u) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L.N) return;
+  const uint32_t m = L.nbmask[n];
+  int X, Y, Z;
+  node_xyz(n, L.nx, L.ny, X, Y, Z);
+  T f[19];
+  if (m & NB_SOLID) {
+    for (int i = 0; i < 19; ++i) f[i] = L.fsrc[i * L.N + n];
+  } else {
+    pull(L, L.fsrc, X, Y, Z, n, m, f);
+  }
+  T rb = T(0);
+  for (int i = 0; i < 19; ++i) rb += f[i];
+  T rhoBar, jx, jy, jz, Fx, Fy, Fz;
+  moments(f, rhoBar, jx, jy, jz);
+  FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
+  const T r = T(1) + rhoBar;
+  if (rho) rho[n] = 1.0 + (double)rb;
+  if (u) {
+    u[n] = (jx + T(0.5) * Fx) / r;
+    u[L.N + n] = (jy + T(0.5) * Fy) / r;
+    u[2 * L.N + n] = (jz + T(0.5) * Fz) / r;
+  }
+}
+template <typename T>
+cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s) {
+  k_moments<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L, rho, u);
+  return cudaGetLastError();
+}
+
+// Post-stream populations (unshifted, double) of every node: the state a
+// collide-then-stream solver holds between steps.  Wall nodes read w_i.
+template <typename T>
+__global__ void k_stream_out(const LbmView<T> L, double* out) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L.N) return;
+  const uint32_t m = L.nbmask[n];
+  T f[19];
+  if (m & NB_SOLID) {
+    for (int i = 0; i < 19; ++i) f[i] = T(0);
+  } else {
+    int X, Y, Z;
+    node_xyz(n, L.nx, L.ny, X, Y, Z);
+    pull(L, L.fsrc, X, Y, Z, n, m, f);
+  }
+#pragma unroll
+  for (int i = 0; i < 19; ++i) out[i * L.N + n] = (double)f[i] + wi(i);
+}
+template <typename T>
+cudaError_t launch_stream_out(const LbmView<T>& L, double* out, cudaStream_t s) {
+  k_stream_out<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L, out);
+  return cudaGetLastError();
+}
+
+// Inverse of the pull: store post-collision values in L.fdst such that the
+// next pull yields the given post-stream populations `in` (unshifted double
+// [19][N]); with `in` null the populations are the equilibrium of (rho, u).
+// Every stored slot has exactly one reader, so each is written once.
+template <typename T>
+__global__ void k_stream_in(const LbmView<T> L, const double* in, double rho, double ux, double uy, double uz) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= L.N) return;
+  const uint32_t m = L.nbmask[n];
+  const long long N = L.N;
+  if (m & NB_SOLID) {
+    for (int i = 0; i < 19; ++i) L.fdst[i * N + n] = T(0);
+    return;
+  }
+  int X, Y, Z;
+  node_xyz(n, L.nx, L.ny, X, Y, Z);
+  const Nbr nb(X, Y, Z, L.nx, L.ny, L.nz);
+  const uint32_t cls = m >> NB_CLASS_SHIFT;
+  const double uu = ux * ux + uy * uy + uz * uz;
+#pragma unroll
+  for (int j = 0; j < 19; ++j) {
+    double fj;
+    if (in) {
+      fj = in[j * N + n] - wi(j);
+    } else {
+      const double cu = cxi(j) * ux + cyi(j) * uy + czi(j) * uz;
+      fj = wi(j) * ((rho - 1.0) + rho * (3.0 * cu + 4.5 * cu * cu - 1.5 * uu));
+    }
+    if (j == 0) {
+      L.fdst[n] = (T)fj;
+      continue;
+    }
+    const int i = oppi(j);
+    if (m & (1u << (i - 1))) {
+      const uint32_t c = wall_class(L, i, X, Y, Z, nb, cls);
+      const double cuw = cxi(i) * (double)L.uw[c][0] + cyi(i) * (double)L.uw[c][1] + czi(i) * (double)L.uw[c][2];
+      L.fdst[i * N + n] = (T)(fj + 6.0 * wi(i) * cuw);
+    } else {
+      const int sx = cxi(j) > 0 ? nb.xm : (cxi(j) < 0 ? nb.xp : X);
+      const int sy = cyi(j) > 0 ? nb.ym : (cyi(j) < 0 ? nb.yp : Y);
+      const int sz = czi(j) > 0 ? nb.zm : (czi(j) < 0 ? nb.zp : Z);
+      L.fdst[j * N + ((long long)sx + (long long)L.nx * ((long long)sy + (long long)L.ny * sz))] = (T)fj;
+    }
+  }
+}
+template <typename T>
+cudaError_t launch_stream_in(const LbmView<T>& L, const double* in, double rho, const double* u3, cudaStream_t s) {
+  k_stream_in<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L, in, rho, u3 ? u3[0] : 0.0, u3 ? u3[1] : 0.0,
+                                                               u3 ? u3[2] : 0.0);
+  return cudaGetLastError();
+}
+
+// force field <-> host layout [3][N] double
+template <typename T>
+__global__ void k_field_out(const T* F, double* out, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  T x, y, z;
+  FieldLayout<T>::load(F, N, n, x, y, z);
+  out[n] = x;
+  out[N + n] = y;
+  out[2 * N + n] = z;
+}
+template <typename T>
+__global__ void k_field_in(const double* in, T* F, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  FieldLayout<T>::store(F, N, n, (T)in[n], (T)in[N + n], (T)in[2 * N + n]);
+}
+template <typename T>
+__global__ void k_fill_body(T* F, const T* bodyz, long long plane, int nz, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int z = (int)(n / plane);
+  FieldLayout<T>::store(F, N, n, bodyz[z], bodyz[nz + z], bodyz[2 * nz + z]);
+}
+template <typename T>
+cudaError_t launch_field_out(const T* F, double* out, long long N, cudaStream_t s) {
+  k_field_out<T><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(F, out, N);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_field_in(const double* in, T* F, long long N, cudaStream_t s) {
+  k_field_in<T><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(in, F, N);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_fill_body(T* F, const T* bodyz, long long plane, int nz, long long N, cudaStream_t s) {
+  k_fill_body<T><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(F, bodyz, plane, nz, N);
+  return cudaGetLastError();
+}
+template <typename T>
+size_t field_bytes(long long N) {
+  return (size_t)N * FieldLayout<T>::kComps * sizeof(T);
+}
+
+// vector conversion T <-> double (vertex arrays)
+template <typename T>
+__global__ void k_convert_in(const double* src, T* dst, long long n) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) dst[k] = (T)src[k];
+}
+template <typename T>
+cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream_t s) {
+  k_convert_in<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+#define HC_LAT_INST(T)                                                                                    \
+  template cudaError_t launch_collide_stream<T>(const LbmView<T>&, int, int, cudaStream_t);              \
+  template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                         \
+  template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);             \
+  template cudaError_t launch_stream_out<T>(const LbmView<T>&, double*, cudaStream_t);                   \
+  template cudaError_t launch_stream_in<T>(const LbmView<T>&, const double*, double, const double*,       \
+                                           cudaStream_t);                                                \
+  template cudaError_t launch_field_out<T>(const T*, double*, long long, cudaStream_t);                  \
+  template cudaError_t launch_field_in<T>(const double*, T*, long long, cudaStream_t);                   \
+  template cudaError_t launch_fill_body<T>(T*, const T*, long long, int, long long, cudaStream_t);       \
+  template size_t field_bytes<T>(long long);                                                             \
+  template cudaError_t launch_convert_in<T>(const double*, T*, long long, cudaStream_t);
+HC_LAT_INST(double)
+HC_LAT_INST(float)
+
+}  // namespace hcd
