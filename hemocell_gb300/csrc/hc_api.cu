@@ -92,12 +92,18 @@ struct hc_handle {
   // stepping
   int iter = 0;
   int velocity_every = 1;
-  int tune[8] = {64, 4, 128, 128, 256, 0, 0, 0};  // k1 bx, k1 by, spread bs, ibm bs, mech bs, mech grid
+  // k1 bx (0: row-staged, blocks of whole x-rows), k1 by, spread bs, ibm bs, mech bs, mech grid,
+  // mech variant (0 vertex gather, 1 face/edge scatter)
+  int tune[8] = {64, 2, 128, 128, 384, 0, 0, 0};
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool graph_valid = false;
   long long device_bytes = 0;
   double* scratch = nullptr;  // readback staging
   size_t scratch_bytes = 0;
+  // the spread of the coming step was already done by the last mechanics
+  // pass (fused spread); anything that changes forces, positions or the
+  // force field between steps clears it
+  bool spread_done = false;
   // external vertex forces (HemoCellStretch)
   int next = 0, next_cap = 0;
   int* ext_ids = nullptr;
@@ -157,6 +163,7 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   L.ntag = h->ntag;
   L.unode = (T*)h->unode;
   L.stamp = h->stamp;
+  L.reverse = src;  // alternates with the buffer parity
   L.omega = (T)(1.0 / h->u.tau);
   for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
@@ -336,6 +343,23 @@ int upload_cell_lists(hc_handle* h) {
   return HC_OK;
 }
 
+// After a fused step the next force field holds body force + the next
+// spread.  A change that makes that spread stale restores the field to the
+// body force so the next step spreads afresh.
+int undo_fused_spread(hc_handle* h) {
+  if (!h->spread_done) return HC_OK;
+  const long long plane = (long long)h->nx * h->ny;
+  if (h->f64)
+    HC_CUDA(h, hcd::launch_fill_body<double>((double*)h->F[h->cur], (const double*)h->bodyz, plane, h->nz, h->N,
+                                             h->stream));
+  else
+    HC_CUDA(h, hcd::launch_fill_body<float>((float*)h->F[h->cur], (const float*)h->bodyz, plane, h->nz, h->N,
+                                            h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->spread_done = false;
+  return HC_OK;
+}
+
 // ----- stage launchers (enqueue only) -------------------------------------
 template <typename T>
 int enq_spread(hc_handle* h) {
@@ -369,8 +393,19 @@ int enq_interp_advance(hc_handle* h, int do_interp, int do_advance, int mark = 0
   return HC_OK;
 }
 
+// The next spread can be fused into this mechanics pass when the batched
+// vertex-centric kernel handles every cell this step, every type is due
+// every step and no external vertex force is added before the spread.
+bool fusable(hc_handle* h) {
+  if (h->p.launch != HC_LAUNCH_BATCHED || h->tune[6] != 0 || h->next > 0 || h->ncells == 0) return false;
+  if (h->velocity_every != 1) return false;
+  for (TypeSlot& ts : h->types)
+    if (ts.every != 1) return false;
+  return true;
+}
+
 template <typename T>
-int enq_mechanics(hc_handle* h, bool forced) {
+int enq_mechanics(hc_handle* h, bool forced, bool fuse = false) {
   bool all_due = true;
   for (TypeSlot& ts : h->types)
     if (!(forced || h->iter % ts.every == 0)) all_due = false;
@@ -379,14 +414,18 @@ int enq_mechanics(hc_handle* h, bool forced) {
   M.cell_voff = h->cell_voff;
   M.types = h->dtypes;
   M.vv = vertex_view<T>(h);
+  M.fuse_spread = 0;
+  M.L = lbm_view<T>(h, h->cur, h->cur);  // Fcur = the next step's force field
+  M.f_limit = (T)h->u.f_limit;
   if (h->p.launch == HC_LAUNCH_BATCHED && all_due && h->ncells > 0) {
+    M.fuse_spread = fuse ? 1 : 0;
     int maxnv = 0;
     for (TypeSlot& ts : h->types)
       if (!ts.cells.empty()) maxnv = std::max(maxnv, ts.tc.nv);
     M.cells = h->dcells_all;
     M.ncells = h->ncells;
     M.dyn_smem = (int)hcd::mechanics_smem_bytes<T>(maxnv);
-    HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], h->tune[5], h->stream));
+    HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], h->tune[5], h->tune[6], h->stream));
     return HC_OK;
   }
   for (TypeSlot& ts : h->types) {
@@ -394,7 +433,7 @@ int enq_mechanics(hc_handle* h, bool forced) {
     M.cells = ts.dcells;
     M.ncells = (int)ts.cells.size();
     M.dyn_smem = (int)hcd::mechanics_smem_bytes<T>(ts.tc.nv);
-    HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], 0, h->stream));
+    HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], 0, h->tune[6], h->stream));
   }
   return HC_OK;
 }
@@ -404,10 +443,12 @@ int enq_mechanics(hc_handle* h, bool forced) {
 template <typename T>
 int enq_step(hc_handle* h) {
   int rc;
-  if ((rc = enq_spread<T>(h)) != HC_OK) return rc;
+  if (!h->spread_done && (rc = enq_spread<T>(h)) != HC_OK) return rc;
   if ((rc = enq_collide<T>(h)) != HC_OK) return rc;
   if ((rc = enq_interp_advance<T>(h, h->iter % h->velocity_every == 0, 1)) != HC_OK) return rc;
-  if ((rc = enq_mechanics<T>(h, false)) != HC_OK) return rc;
+  const bool fuse = fusable(h);
+  if ((rc = enq_mechanics<T>(h, false, fuse)) != HC_OK) return rc;
+  h->spread_done = fuse;
   h->iter++;
   return HC_OK;
 }
@@ -423,6 +464,7 @@ bool graph_eligible(hc_handle* h) {
 template <typename T>
 int build_graph(hc_handle* h, int parity) {
   const int save_cur = h->cur, save_iter = h->iter;
+  const bool save_sd = h->spread_done;
   h->cur = parity;
   cudaGraph_t g = nullptr;
   HC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -431,6 +473,7 @@ int build_graph(hc_handle* h, int parity) {
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   h->cur = save_cur;
   h->iter = save_iter;
+  h->spread_done = save_sd;
   if (rc != HC_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -445,7 +488,11 @@ int build_graph(hc_handle* h, int parity) {
 template <typename T>
 int run_steps(hc_handle* h, int nsteps) {
   int rc;
-  if (graph_eligible(h) && nsteps >= 2) {
+  if (graph_eligible(h) && nsteps >= 3 && fusable(h) && !h->spread_done) {
+    if ((rc = enq_step<T>(h)) != HC_OK) return rc;  // leaves the next spread done
+    nsteps--;
+  }
+  if (graph_eligible(h) && nsteps >= 2 && (!fusable(h) || h->spread_done)) {
     if (!h->graph_valid) {
       invalidate_graph(h);
       if ((rc = build_graph<T>(h, 0)) != HC_OK) return rc;
@@ -465,6 +512,10 @@ int run_steps(hc_handle* h, int nsteps) {
 
 template <typename T>
 int run_stage(hc_handle* h, int stage) {
+  if (stage != HC_STAGE_BIN) {
+    int rc0 = undo_fused_spread(h);
+    if (rc0 != HC_OK) return rc0;
+  }
   switch (stage) {
     case HC_STAGE_SPREAD:
       return enq_spread<T>(h);
@@ -516,6 +567,8 @@ int add_cells_positions(hc_handle* h, int type, int n, const std::vector<double>
     if (!std::isfinite(q)) return fail(h, HC_ERR_NUMERIC, "non-finite vertex position");
   invalidate_graph(h);
   int rc;
+  // new vertices need the spread to tag their stencils
+  if ((rc = undo_fused_spread(h)) != HC_OK) return rc;
   if (need > h->Vcap) {
     long long nc = std::max<long long>(need, 2 * h->Vcap);
     nc = std::max<long long>(nc, 1024);
@@ -656,11 +709,12 @@ int autotune(hc_handle* h, const char* cache) {
     HC_CUDA(h, cudaMemcpyAsync(sv, h->v, vb, cudaMemcpyDeviceToDevice, h->stream));
     HC_CUDA(h, cudaMemcpyAsync(sf, h->fv, vb, cudaMemcpyDeviceToDevice, h->stream));
   }
-  const int k1[][2] = {{32, 4}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {256, 1}, {32, 8}};
+  const int k1[][2] = {{0, 1}, {0, 2}, {0, 4}, {32, 4}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {256, 1}, {32, 8}};
   float best = 1e30f;
   int bx = h->tune[0], by = h->tune[1];
   for (auto& c : k1) {
     if (c[0] > 2 * h->nx && c[0] > 32) continue;
+    if (c[0] == 0 && h->nx * c[1] > 256) continue;
     h->tune[0] = c[0];
     h->tune[1] = c[1];
     float t = time_it<T>(h, 5, 0);
@@ -686,24 +740,28 @@ int autotune(hc_handle* h, const char* cache) {
     h->tune[3] = bb;
     h->tune[2] = bb;
     best = 1e30f;
-    int mb = h->tune[4], mg = h->tune[5];
+    int mb = h->tune[4], mg = h->tune[5], mv = h->tune[6];
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
-    for (int bs : {128, 256, 512, 1024})
-      for (int gr : {0, 2 * sms, 4 * sms}) {
-        if (bs > 512 && h->f64) continue;
-        if (gr != 0 && h->p.launch != HC_LAUNCH_BATCHED) continue;
-        h->tune[4] = bs;
-        h->tune[5] = gr;
-        float t = time_it<T>(h, 3, 2);
-        if (t < best) {
-          best = t;
-          mb = bs;
-          mg = gr;
+    for (int var : {0, 1})
+      for (int bs : {128, 256, 384, 512, 768})
+        for (int gr : {0, 2 * sms}) {
+          if (bs > (h->f64 ? 384 : 768)) continue;
+          if (gr != 0 && h->p.launch != HC_LAUNCH_BATCHED) continue;
+          h->tune[4] = bs;
+          h->tune[5] = gr;
+          h->tune[6] = var;
+          float t = time_it<T>(h, 3, 2);
+          if (t < best) {
+            best = t;
+            mb = bs;
+            mg = gr;
+            mv = var;
+          }
         }
-      }
     h->tune[4] = mb;
     h->tune[5] = mg;
+    h->tune[6] = mv;
     HC_CUDA(h, cudaMemcpyAsync(h->v, sv, vb, cudaMemcpyDeviceToDevice, h->stream));
     HC_CUDA(h, cudaMemcpyAsync(h->fv, sf, vb, cudaMemcpyDeviceToDevice, h->stream));
   }
@@ -898,6 +956,7 @@ int hc_derived_units(const hc_handle* h, double* out) {
 
 int hc_set_flags(hc_handle* h, const uint8_t* flags) {
   if (!h || !flags) return HC_ERR_INVALID;
+  if (int rc0 = undo_fused_spread(h)) return rc0;
   invalidate_graph(h);
   return restore_populations(h, [&]() {
     std::memcpy(h->hflag.data(), flags, h->N);
@@ -917,6 +976,7 @@ int hc_set_wall_velocity(hc_handle* h, int cls, const double* u3) {
 
 int hc_set_body_force(hc_handle* h, int mode, const double* p) {
   if (!h) return HC_ERR_INVALID;
+  h->spread_done = false;  // the force field is refilled with the body force
   if (mode < HC_BODY_NONE || mode > HC_BODY_KOLMOGOROV) return fail(h, HC_ERR_INVALID, "unknown body-force mode");
   if (mode != HC_BODY_NONE && !p) return fail(h, HC_ERR_INVALID, "body-force parameters missing");
   h->body_mode = mode;
@@ -973,7 +1033,9 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
     return o;
   };
   const size_t o_tris = put_i(c.tris), o_edges = put_i(c.edges), o_bt = put_i(c.bend_tris),
-               o_bo = put_i(c.bend_outer), o_ring = put_i(c.ring), o_rn = put_i(c.ring_n), o_in = put_i(c.inner);
+               o_bo = put_i(c.bend_outer), o_ring = put_i(c.ring), o_rn = put_i(c.ring_n), o_in = put_i(c.inner),
+               o_vf = put_i(c.vface), o_ve = put_i(c.vedge), o_vo = put_i(c.vopp), o_vio = put_i(c.vinner_off),
+               o_vi = put_i(c.vinner), o_sr = put_i(c.slot_rot);
   while (iv.size() % 2) iv.push_back(0);
   std::vector<double> dv;
   auto put_d = [&](const std::vector<double>& a) {
@@ -982,7 +1044,7 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
     return o;
   };
   const size_t o_a0 = put_d(c.tri_a0), o_l0 = put_d(c.edge_l0), o_ang = put_d(c.edge_angle0),
-               o_pd = put_d(c.patch_d0), o_il = put_d(c.inner_l0);
+               o_pd = put_d(c.patch_d0), o_il = put_d(c.inner_l0), o_sa = put_d(c.slot_a0), o_sl = put_d(c.slot_l0);
   std::vector<float> fv(dv.begin(), dv.end());
   const size_t ib = 4 * iv.size(), db = 8 * std::max<size_t>(dv.size(), 1), fb = 4 * std::max<size_t>(fv.size(), 1);
   HC_CUDA(h, dalloc(h, &ts.blob, ib + db + fb));
@@ -1005,6 +1067,16 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
   d.ring = ibase + o_ring;
   d.ring_n = ibase + o_rn;
   d.inner = ibase + o_in;
+  d.vface = ibase + o_vf;
+  d.vedge = ibase + o_ve;
+  d.vopp = ibase + o_vo;
+  d.vinner_off = ibase + o_vio;
+  d.vinner = ibase + o_vi;
+  d.slot_rot = ibase + o_sr;
+  d.slot_a0 = dbase + o_sa;
+  d.slot_l0 = dbase + o_sl;
+  d.slot_a0f = fbase + o_sa;
+  d.slot_l0f = fbase + o_sl;
   d.tri_a0 = dbase + o_a0;
   d.edge_l0 = dbase + o_l0;
   d.edge_angle0 = dbase + o_ang;
@@ -1065,6 +1137,7 @@ int hc_set_timescales(hc_handle* h, const int* every, int ntypes, int velocity_e
     if (every[t] % velocity_every != 0)
       return fail(h, HC_ERR_INVALID, "velocity timescale separation cannot divide all material timescale separations");
   }
+  if (int rc0 = undo_fused_spread(h)) return rc0;
   for (int t = 0; t < ntypes; ++t) h->types[t].every = every[t];
   h->velocity_every = velocity_every;
   invalidate_graph(h);
@@ -1073,6 +1146,7 @@ int hc_set_timescales(hc_handle* h, const int* every, int ntypes, int velocity_e
 
 int hc_set_vertex_forces(hc_handle* h, int n, const int* ids, const double* forces) {
   if (!h || n < 0 || (n > 0 && (!ids || !forces))) return HC_ERR_INVALID;
+  if (int rc0 = undo_fused_spread(h)) return rc0;
   for (int k = 0; k < n; ++k)
     if (ids[k] < 0 || ids[k] >= h->nvert) return fail(h, HC_ERR_INVALID, "vertex id out of range");
   if (n > h->next_cap) {
@@ -1182,6 +1256,7 @@ int hc_read_force_field(hc_handle* h, double* F, int which) {
 
 int hc_write_force_field(hc_handle* h, const double* F) {
   if (!h || !F) return HC_ERR_INVALID;
+  h->spread_done = false;  // the field is overwritten: it holds no spread
   int rc;
   if ((rc = ensure_scratch(h, sizeof(double) * 3 * h->N)) != HC_OK) return rc;
   HC_CUDA(h, cudaMemcpyAsync(h->scratch, F, 8 * 3 * h->N, cudaMemcpyHostToDevice, h->stream));
@@ -1210,6 +1285,7 @@ int hc_read_vertices(hc_handle* h, double* x, double* v, double* f) {
 
 int hc_write_vertices(hc_handle* h, const double* x, const double* v, const double* f) {
   if (!h) return HC_ERR_INVALID;
+  if (int rc0 = undo_fused_spread(h)) return rc0;
   if (h->nvert == 0) return HC_OK;
   int rc;
   if (x && (rc = write3(h, h->x, 8, x)) != HC_OK) return rc;
@@ -1234,9 +1310,12 @@ int hc_read_cells(hc_handle* h, int* alive, double* volume) {
       const double* X = x.data() + 3 * (size_t)h->h_cell_voff[c];
       double vol = 0;
       for (int k = 0; k < tc.nf; ++k) {
-        const double* v0 = X + 3 * tc.tris[3 * k];
-        const double* v1 = X + 3 * tc.tris[3 * k + 1];
-        const double* v2 = X + 3 * tc.tris[3 * k + 2];
+        double v0[3], v1[3], v2[3];
+        for (int a = 0; a < 3; ++a) {
+          v0[a] = X[3 * tc.tris[3 * k] + a] - X[a];
+          v1[a] = X[3 * tc.tris[3 * k + 1] + a] - X[a];
+          v2[a] = X[3 * tc.tris[3 * k + 2] + a] - X[a];
+        }
         vol += (-v2[0] * v1[1] * v0[2] + v1[0] * v2[1] * v0[2] + v2[0] * v0[1] * v1[2] - v0[0] * v2[1] * v1[2] -
                 v1[0] * v0[1] * v2[2] + v0[0] * v1[1] * v2[2]);
       }
@@ -1313,12 +1392,13 @@ int hc_get_tuning(hc_handle* h, int* out8) {
 
 int hc_set_tuning(hc_handle* h, const int* in8) {
   if (!h || !in8) return HC_ERR_INVALID;
-  if (in8[0] <= 0 || in8[1] <= 0 || in8[0] * in8[1] > 256 || in8[0] % 32 != 0)
-    return fail(h, HC_ERR_INVALID, "collide-stream block must be a multiple of 32 wide and at most 256 threads");
+  if (in8[0] < 0 || in8[1] <= 0 || in8[0] * in8[1] > 256 || in8[0] % 32 != 0)
+    return fail(h, HC_ERR_INVALID, "collide-stream block must be 0 (whole rows) or a multiple of 32 wide, at most 256 threads");
   for (int k = 2; k <= 3; ++k)
     if (in8[k] <= 0 || in8[k] > 512 || in8[k] % 32 != 0) return fail(h, HC_ERR_INVALID, "bad block size");
-  if (in8[4] <= 0 || in8[4] > (h->f64 ? 512 : 1024) || in8[4] % 32 != 0)
+  if (in8[4] <= 0 || in8[4] > (h->f64 ? 384 : 768) || in8[4] % 32 != 0)
     return fail(h, HC_ERR_INVALID, "bad mechanics block size");
+  if (in8[6] != 0 && in8[6] != 1) return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather) or 1 (scatter)");
   std::memcpy(h->tune, in8, sizeof(h->tune));
   invalidate_graph(h);
   return HC_OK;

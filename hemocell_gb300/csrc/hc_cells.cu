@@ -316,6 +316,43 @@ __device__ __forceinline__ void add3(T* s, int k, V3t<T> v) {
   atomicAdd(s + 3 * k + 1, v.y);
   atomicAdd(s + 3 * k + 2, v.z);
 }
+// Division and normalisation: IEEE in FP64 (the plain form follows the
+// reference's arithmetic), fast reciprocal / rsqrt in the FP32 mixed form.
+template <typename T>
+__device__ __forceinline__ T fdiv(T a, T b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float fdiv<float>(float a, float b) {
+  return __fdividef(a, b);
+}
+// v / |v| with |v| returned in len (len = 0 leaves v unnormalised)
+template <typename T>
+__device__ __forceinline__ V3t<T> normalized(V3t<T> v, T& len) {
+  len = vnorm(v);
+  if (len == T(0)) return v;
+  return {v.x / len, v.y / len, v.z / len};
+}
+template <>
+__device__ __forceinline__ V3t<float> normalized<float>(V3t<float> v, float& len) {
+  const float d = vdot(v, v);
+  if (d == 0.f) {
+    len = 0.f;
+    return v;
+  }
+  const float inv = rsqrtf(d);
+  len = d * inv;
+  return {v.x * inv, v.y * inv, v.z * inv};
+}
+template <typename T>
+__device__ __forceinline__ T third(T a) {
+  return a / T(3);
+}
+template <>
+__device__ __forceinline__ float third<float>(float a) {
+  return a * (1.0f / 3.0f);
+}
+
 template <typename T>
 __device__ __forceinline__ V3t<T> unit_normal(V3t<T> a, V3t<T> b, V3t<T> c) {
   V3t<T> n = vcross(b - a, c - a);
@@ -353,17 +390,281 @@ __device__ __forceinline__ float rest_value<float>(const double*, const float* f
 
 template <typename T>
 size_t mechanics_smem_bytes(int nv) {
-  return 34 * sizeof(double) + 6 * (size_t)nv * sizeof(T);
+  return 34 * sizeof(double) + 6 * (size_t)nv * sizeof(T) + (size_t)nv;
 }
 
-// One CTA per cell (grid-stride over the cell list).  Pass A runs the faces
+// One CTA per cell (grid-stride over the cell list), vertex-centric: each
+// thread owns vertices and sums, in a fixed order, every contribution the
+// reference's face / edge / vertex loops deposit on them
+// (rbcHighOrderModel.cpp:56-204, pltSimpleModel.cpp:59-205,
+// wbcHighOrderModel.cpp:60-223).  Phase 1 sums the face volume terms and
+// evaluates each vertex's own bending force into shared memory; after the
+// block reduction of the volume, phase 2 gathers for each vertex: area and
+// volume forces of its incident faces, link and membrane viscosity of its
+// ring edges, the neighbours' bending reactions, the platelet dihedral terms
+// of its incident and opposite edges, and its inner links.  No atomics: the
+// forces are bit-reproducible.
+template <typename T>
+struct Face {
+  V3t<T> n;  // unit normal
+  T area;
+  V3t<T> cen;
+};
+
+template <typename T>
+__device__ __forceinline__ Face<T> face_geometry(const T* sx, const TypeDev& t, int k) {
+  const int i0 = t.tris[3 * k], i1 = t.tris[3 * k + 1], i2 = t.tris[3 * k + 2];
+  const V3t<T> v0 = ld3(sx, i0), v1 = ld3(sx, i1), v2 = ld3(sx, i2);
+  Face<T> F;
+  V3t<T> n = vcross(v1 - v0, v2 - v0);
+  const T nn = vnorm(n);
+  if (nn != T(0)) {
+    F.area = T(0.5) * nn;
+    F.n = {n.x / nn, n.y / nn, n.z / nn};
+  } else {
+    F.area = T(0);
+    F.n = {T(0), T(0), T(0)};
+  }
+  F.cen = {(v0.x + v1.x + v2.x) / T(3), (v0.y + v1.y + v2.y) / T(3), (v0.z + v1.z + v2.z) / T(3)};
+  return F;
+}
+
+// platelet dihedral bending force of edge e (pltSimpleModel.cpp:156-182),
+// +bfv on its end points, -bfv on the two outer points
+template <typename T>
+__device__ __forceinline__ V3t<T> plt_bending(const T* sx, const TypeDev& t, int e) {
+  const int a = t.edges[2 * e], b = t.edges[2 * e + 1];
+  const V3t<T> ev = ld3(sx, b) - ld3(sx, a);
+  const T L = vnorm(ev);
+  const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
+  const int* A = t.tris + 3 * t.bend_tris[2 * e];
+  const int* B = t.tris + 3 * t.bend_tris[2 * e + 1];
+  const V3t<T> V1 = unit_normal(ld3(sx, A[0]), ld3(sx, A[1]), ld3(sx, A[2]));
+  const V3t<T> V2 = unit_normal(ld3(sx, B[0]), ld3(sx, B[1]), ld3(sx, B[2]));
+  const T angle = atan2(vdot(vcross(V1, V2), uv), vdot(V1, V2));
+  const T af = angle - rest_value<T>(t.edge_angle0, t.edge_angle0f, e);
+  const T fm = (T)t.k_bend * (af + af / fabs(T(kMaxPltBend) - af * af));
+  return vscale(V1 + V2, fm * T(0.5));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const MechView<T> M) {
+  extern __shared__ double smem_d[];
+  __shared__ TypeDev tshared;
+  double* red = smem_d;  // 34 doubles
+  T* sx = reinterpret_cast<T*>(smem_d + 34);
+  const VertexView<T>& vv = M.vv;
+  const long long V = vv.V;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  constexpr bool kF64 = sizeof(T) == 8;
+  for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
+    const int cell = M.cells[ci];
+    __syncthreads();  // previous cell fully written out
+    if (tid == 0) tshared = M.types[M.cell_type[cell]];
+    __syncthreads();
+    const TypeDev& t = tshared;
+    const int nv = t.nv;
+    const int voff = M.cell_voff[cell];
+    T* sbf = sx + 3 * nv;  // own bending force per vertex
+    uint8_t* srn = reinterpret_cast<uint8_t*>(sbf + 3 * nv);  // valence per vertex
+    const bool alive = vv.alive[cell] != 0;
+    for (int k = tid; k < nv; k += bs) srn[k] = (uint8_t)t.ring_n[k];
+    // positions relative to the cell's vertex 0 (translation invariant forces;
+    // the volume sum stays well conditioned far from the origin)
+    const double r0x = vv.x[voff], r0y = vv.x[V + voff], r0z = vv.x[2 * V + voff];
+    for (int k = tid; k < nv; k += bs) {
+      sx[3 * k] = (T)(vv.x[voff + k] - r0x);
+      sx[3 * k + 1] = (T)(vv.x[V + voff + k] - r0y);
+      sx[3 * k + 2] = (T)(vv.x[2 * V + voff + k] - r0z);
+    }
+    __syncthreads();
+    if (!alive) {
+      for (int k = tid; k < nv; k += bs) {
+        vv.f[voff + k] = T(0);
+        vv.f[V + voff + k] = T(0);
+        vv.f[2 * V + voff + k] = T(0);
+      }
+      continue;
+    }
+    // --- phase 1: face volume terms, own bending force (rbcHighOrderModel.cpp:62-68, :127-157)
+    double vol = 0.0;
+    for (int k = tid; k < t.nf; k += bs) {
+      const V3t<T> v0 = ld3(sx, t.tris[3 * k]), v1 = ld3(sx, t.tris[3 * k + 1]), v2 = ld3(sx, t.tris[3 * k + 2]);
+      if (kF64) {
+        const double v210 = (double)v2.x * v1.y * v0.z, v120 = (double)v1.x * v2.y * v0.z;
+        const double v201 = (double)v2.x * v0.y * v1.z, v021 = (double)v0.x * v2.y * v1.z;
+        const double v102 = (double)v1.x * v0.y * v2.z, v012 = (double)v0.x * v1.y * v2.z;
+        vol += (-v210 + v120 + v201 - v021 - v102 + v012);
+      } else {
+        // v0 . ((v1-v0) x (v2-v0)) == v0 . (v1 x v2): FP32 term, FP64 sum
+        vol += (double)vdot(v0, vcross(v1 - v0, v2 - v0));
+      }
+    }
+    if (t.model != 1) {
+      for (int i = tid; i < nv; i += bs) {
+        const int rn = t.ring_n[i];
+        const int* rg = t.ring + 6 * i;
+        const V3t<T> xi = ld3(sx, i);
+        V3t<T> sum = {T(0), T(0), T(0)};
+        for (int j = 0; j < rn; ++j) sum = sum + ld3(sx, rg[j]);
+        const V3t<T> mid = {fdiv(sum.x, (T)rn), fdiv(sum.y, (T)rn), fdiv(sum.z, (T)rn)};
+        const V3t<T> dev = mid - xi;
+        V3t<T> pn = {T(0), T(0), T(0)};
+        V3t<T> a = ld3(sx, rg[0]) - xi;
+        const V3t<T> first = a;
+        for (int j = 0; j < rn; ++j) {
+          const V3t<T> b = (j + 1 < rn) ? ld3(sx, rg[j + 1]) - xi : first;
+          T l;
+          pn = pn + normalized(vcross(a, b), l);
+          a = b;
+        }
+        T pl;
+        pn = normalized(pn, pl);
+        const T ndev = vdot(pn, dev);
+        const T dDev = fdiv(ndev - rest_value<T>(t.patch_d0, t.patch_d0f, i), (T)t.edge_mean_eq);
+        const V3t<T> bf = vscale(pn, (T)t.k_bend * (dDev + fdiv(dDev, fabs(T(kMaxBend) - dDev * dDev))));
+        sbf[3 * i] = bf.x;
+        sbf[3 * i + 1] = bf.y;
+        sbf[3 * i + 2] = bf.z;
+      }
+    }
+    block_sum<T>(vol, red);  // red[32] = sum over the block (synchronises)
+    // volume constraint in FP64 (rbcHighOrderModel.cpp:100-104), by one thread
+    if (tid == 0) {
+      const double volume = red[32] * (1.0 / 6.0);
+      const double vfr = (volume - t.volume_eq) / t.volume_eq;
+      const double vf = -t.k_volume * vfr / fabs(kMaxVol - vfr * vfr);
+      red[33] = vf;
+      red[31] = vf / t.area_mean_eq;
+    }
+    __syncthreads();
+    const T vforce = (T)red[33];
+    const T vforce_per_area = (T)red[31];
+    const T area_mean = (T)t.area_mean_eq;
+    const bool visc = (t.model != 0) || (t.eta_m != 0.0);
+    // --- phase 2: gather per vertex
+    for (int i = tid; i < nv; i += bs) {
+      const int rn = t.ring_n[i];
+      const V3t<T> xi = ld3(sx, i);
+      V3t<T> f = {T(0), T(0), T(0)};
+      V3t<T> vi = {T(0), T(0), T(0)};
+      if (visc) vi = {vv.v[voff + i], vv.v[V + voff + i], vv.v[2 * V + voff + i]};
+      int rs[6], rot[6];
+      T a0s[6], l0s[6];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        if (j < rn) {
+          rs[j] = t.ring[6 * i + j];
+          rot[j] = t.slot_rot[6 * i + j];
+          a0s[j] = rest_value<T>(t.slot_a0, t.slot_a0f, 6 * i + j);
+          l0s[j] = rest_value<T>(t.slot_l0, t.slot_l0f, 6 * i + j);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        if (j >= rn) break;
+        const int r = rs[j];
+        const int r1 = rs[j + 1 < rn ? j + 1 : 0];
+        // incident face (i, r, r1) in the reference's corner order: area force
+        // on this corner and the face's volume force
+        const V3t<T> xr = ld3(sx, r), xr1 = ld3(sx, r1);
+        const V3t<T> c0 = rot[j] == 0 ? xi : (rot[j] == 1 ? xr1 : xr);
+        const V3t<T> c1 = rot[j] == 0 ? xr : (rot[j] == 1 ? xi : xr1);
+        const V3t<T> c2 = rot[j] == 0 ? xr1 : (rot[j] == 1 ? xr : xi);
+        Face<T> F;
+        {
+          T nn;
+          const V3t<T> n = normalized(vcross(c1 - c0, c2 - c0), nn);
+          if (nn != T(0)) {
+            F.area = T(0.5) * nn;
+            F.n = n;
+          } else {
+            F.area = T(0);
+            F.n = {T(0), T(0), T(0)};
+          }
+          F.cen = {third(c0.x + c1.x + c2.x), third(c0.y + c1.y + c2.y), third(c0.z + c1.z + c2.z)};
+        }
+        const T a0 = a0s[j];
+        const T ar = fdiv(F.area - a0, a0);
+        const T afm = (T)t.k_area * (ar + fdiv(ar, fabs(T(kMaxArea) - ar * ar)));
+        f = f + vscale(F.cen - xi, afm);
+        if (kF64) f = f + vscale(vscale(F.n, vforce), F.area / area_mean);
+        else f = f + vscale(F.n, vforce_per_area * F.area);
+        // ring edge (i, r): link force toward r when stretched, viscosity
+        const int e = t.vedge[6 * i + j];
+        T L;
+        const V3t<T> uv = normalized(xr - xi, L);
+        const T l0 = l0s[j];
+        const T ef = fdiv(L - l0, l0);
+        f = f + vscale(uv, (T)t.k_link * (ef + fdiv(ef, fabs(T(kMaxLink) - ef * ef))));
+        if (visc) {
+          const V3t<T> vr = {vv.v[voff + r], vv.v[V + voff + r], vv.v[2 * V + voff + r]};
+          V3t<T> fv = vscale(vscale(uv, vdot(vr - vi, uv)), (T)t.eta_m);
+          const T mm = vnorm(fv);
+          if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
+          f = f + fv;
+        }
+        if (t.model != 1) {
+          // neighbour's bending reaction -bf_r / n_r
+          const T rnr = (T)srn[r];
+          f = f + V3t<T>{fdiv(-sbf[3 * r], rnr), fdiv(-sbf[3 * r + 1], rnr), fdiv(-sbf[3 * r + 2], rnr)};
+        } else {
+          // platelet dihedral terms: end point of edge e, outer point of the opposite edge
+          f = f + plt_bending(sx, t, e);
+          f = f - plt_bending(sx, t, t.vopp[6 * i + j]);
+        }
+      }
+      if (t.model != 1) f = f + ld3(sbf, i);
+      // inner links (pltSimpleModel.cpp:188-205, wbcHighOrderModel.cpp:202-223)
+      for (int q = t.vinner_off[i]; q < t.vinner_off[i + 1]; ++q) {
+        const int e = t.vinner[q];
+        const int o = t.inner[2 * e] == i ? t.inner[2 * e + 1] : t.inner[2 * e];
+        const V3t<T> ev = ld3(sx, o) - xi;
+        const T L = vnorm(ev);
+        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};  // toward the partner
+        if (t.model == 1) {
+          const T l0 = rest_value<T>(t.inner_l0, t.inner_l0f, e);
+          f = f + vscale(uv, (T)t.k_link * T(5) * ((L - l0) / l0));
+        } else if (t.model == 2) {
+          if (L < T(2) * (T)t.radius) f = f - vscale(vscale(uv, T(1) - L / (T(2) * (T)t.radius)), (T)t.k_cyto);
+          if (L < T(2) * (T)t.core_radius)
+            f = f - vscale(vscale(uv, T(1) - L / (T(2) * (T)t.core_radius)), (T)t.k_inner_rigid);
+        }
+      }
+      vv.f[voff + i] = f.x;
+      vv.f[V + voff + i] = f.y;
+      vv.f[2 * V + voff + i] = f.z;
+      if (M.fuse_spread) {
+        // spreadParticleForce of the next step (core/hemoCellParticleField.cpp:841-863);
+        // the stored force stays unclamped as after the reference's constitutive model
+        T mag = f.x * f.x;
+        mag += f.y * f.y;
+        mag += f.z * f.z;
+        mag = sqrt(mag);
+        if (mag > M.f_limit) f = vscale(f, M.f_limit / mag);
+        Kern<T> K;
+        ibm_weights(M.L, vv.x[voff + i], vv.x[V + voff + i], vv.x[2 * V + voff + i], K);
+        const uint32_t stamp = *M.L.stamp;
+        T* F = const_cast<T*>(M.L.Fcur);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (K.node[j] < 0) continue;
+          M.L.ntag[K.node[j]] = stamp;
+          FieldLayout<T>::add(F, M.L.N, K.node[j], f.x * K.w[j], f.y * K.w[j], f.z * K.w[j]);
+        }
+      }
+    }
+  }
+}
+
+// Scatter variant (selected by the tuner): one CTA per cell.  Pass A runs the faces
 // (volume terms, area force); after the block reduction of the volume, pass B
 // runs the volume force of every face, the bending of every vertex (RBC,
 // WBC), every edge (link, membrane viscosity, platelet dihedral bending) and
 // every inner link as one merged item loop.  Forces accumulate in shared
 // memory and are written once.
 template <typename T>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) k_mechanics(const MechView<T> M) {
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics_scatter(const MechView<T> M) {
   extern __shared__ double smem_d[];
   __shared__ TypeDev tshared;
   double* red = smem_d;  // 34 doubles
@@ -382,9 +683,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) k_mechanics(const
     const int voff = M.cell_voff[cell];
     T* sf = sx + 3 * nv;
     const bool alive = vv.alive[cell] != 0;
-    // positions: absolute in FP64 (as the reference), relative to vertex 0 in FP32
-    const double r0x = kF64 ? 0.0 : vv.x[voff], r0y = kF64 ? 0.0 : vv.x[V + voff],
-                 r0z = kF64 ? 0.0 : vv.x[2 * V + voff];
+    const double r0x = vv.x[voff], r0y = vv.x[V + voff], r0z = vv.x[2 * V + voff];
     for (int k = tid; k < nv; k += bs) {
       sx[3 * k] = (T)(vv.x[voff + k] - r0x);
       sx[3 * k + 1] = (T)(vv.x[V + voff + k] - r0y);
@@ -564,16 +863,21 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024) k_mechanics(const
 // added, never inside a stream capture).
 template <typename T>
 cudaError_t prepare_mechanics(int smem_bytes) {
-  return cudaFuncSetAttribute(k_mechanics<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  cudaError_t e = cudaFuncSetAttribute(k_mechanics<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_mechanics_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
 }
 
+// variant 0: vertex-centric gather (deterministic), 1: face/edge scatter with
+// shared-memory atomics
 template <typename T>
-cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s) {
+cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, int variant, cudaStream_t s) {
   if (M.ncells <= 0) return cudaSuccess;
   if (bs <= 0) bs = 256;
-  if (bs > (sizeof(T) == 8 ? 512 : 1024)) bs = sizeof(T) == 8 ? 512 : 1024;
+  if (bs > (sizeof(T) == 8 ? 384 : 768)) bs = sizeof(T) == 8 ? 384 : 768;
   if (grid <= 0 || grid > M.ncells) grid = M.ncells;
-  k_mechanics<T><<<grid, bs, M.dyn_smem, s>>>(M);
+  if (variant == 1) k_mechanics_scatter<T><<<grid, bs, M.dyn_smem, s>>>(M);
+  else k_mechanics<T><<<grid, bs, M.dyn_smem, s>>>(M);
   return cudaGetLastError();
 }
 
@@ -791,7 +1095,7 @@ cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, cons
                                                    cudaStream_t);                                              \
   template cudaError_t launch_interp_advance<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&, int, \
                                                 int, int, cudaStream_t);                                       \
-  template cudaError_t launch_mechanics<T>(const MechView<T>&, int, int, cudaStream_t);                        \
+  template cudaError_t launch_mechanics<T>(const MechView<T>&, int, int, int, cudaStream_t);                   \
   template size_t mechanics_smem_bytes<T>(int);                                                                \
   template cudaError_t prepare_mechanics<T>(int);                                                              \
   template cudaError_t launch_soa_to_aos<T>(const T*, double*, long long, int, cudaStream_t);                  \

@@ -165,6 +165,70 @@ __device__ __forceinline__ void moments(const T f[19], T& rhoBar, T& jx, T& jy, 
   jz = (d[3] + d[6]) - d[7] + (d[8] - d[9]);
 }
 
+// Pull through shared memory for a block that holds whole x-rows
+// (blockDim.x == nx): the 10 directions with c_x != 0 are loaded once,
+// aligned, by the lane whose row neighbour needs them, then gathered from
+// shared memory, so every population element is read from HBM at most once
+// and only when the node that pulls it needs it (need_mask of each lane's
+// own node: bit 0 = this node needs its populations).  `buf` holds
+// 10 * blockDim.y * nx values, `msk` blockDim.y * nx words.  All threads of
+// the block must call this (it synchronises twice).
+__host__ __device__ constexpr int xdir_slot(int j) {
+  return j == 1 ? 0 : j == 4 ? 1 : j == 5 ? 2 : j == 6 ? 3 : j == 7 ? 4 : j == 10 ? 5 : j == 13 ? 6 : j == 14 ? 7
+         : j == 15 ? 8 : j == 16 ? 9 : -1;
+}
+
+template <typename T>
+__device__ __forceinline__ void pull_rows(const LbmView<T>& L, const T* __restrict__ src, int X, int Y, int Z,
+                                          long long n, uint32_t m, bool need, T* buf, uint32_t* msk, T f[19]) {
+  const long long N = L.N;
+  const int nx = L.nx;
+  const int ty = threadIdx.y, rowlen = nx, slot_stride = blockDim.y * nx;
+  const Nbr nb(X, Y, Z, L.nx, L.ny, L.nz);
+  // own mask with the need bit folded in (bit 23, the solid bit, is set when not needed)
+  msk[ty * rowlen + X] = need ? (m & ~NB_SOLID) : NB_SOLID;
+  __syncthreads();
+#pragma unroll
+  for (int j = 1; j < 19; ++j) {
+    if (cxi(j) == 0) continue;
+    // destination of the value this lane loads: (X + c_x, same row)
+    const int xd = cxi(j) > 0 ? nb.xp : nb.xm;
+    const uint32_t md = msk[ty * rowlen + xd];
+    const bool used = !(md & NB_SOLID) && !(md & (1u << (oppi(j) - 1)));
+    if (used) {
+      const int sy = cyi(j) > 0 ? nb.ym : (cyi(j) < 0 ? nb.yp : Y);
+      const int sz = czi(j) > 0 ? nb.zm : (czi(j) < 0 ? nb.zp : Z);
+      buf[xdir_slot(j) * slot_stride + ty * rowlen + X] =
+          src[j * N + ((long long)X + (long long)L.nx * ((long long)sy + (long long)L.ny * sz))];
+    }
+  }
+  __syncthreads();
+  if (!need) return;
+  const uint32_t cls = m >> NB_CLASS_SHIFT;
+  f[0] = src[n];
+#pragma unroll
+  for (int j = 1; j < 19; ++j) {
+    const int i = oppi(j);
+    if (m & (1u << (i - 1))) {
+      const uint32_t c = wall_class(L, i, X, Y, Z, nb, cls);
+      const T cuw = T(cxi(i)) * L.uw[c][0] + T(cyi(i)) * L.uw[c][1] + T(czi(i)) * L.uw[c][2];
+      f[j] = src[i * N + n] - T(6.0 * wi(i)) * cuw;
+    } else if (cxi(j) != 0) {
+      const int xs = cxi(j) > 0 ? nb.xm : nb.xp;
+      f[j] = buf[xdir_slot(j) * slot_stride + ty * rowlen + xs];
+    } else {
+      const int sy = cyi(j) > 0 ? nb.ym : (cyi(j) < 0 ? nb.yp : Y);
+      const int sz = czi(j) > 0 ? nb.zm : (czi(j) < 0 ? nb.zp : Z);
+      f[j] = src[j * N + ((long long)X + (long long)L.nx * ((long long)sy + (long long)L.ny * sz))];
+    }
+  }
+}
+
+template <typename T>
+size_t pull_rows_smem(int nx, int by) {
+  return (size_t)10 * by * nx * sizeof(T) + (size_t)by * nx * sizeof(uint32_t);
+}
+
 __device__ __forceinline__ void node_xyz(long long n, int nx, int ny, int& X, int& Y, int& Z) {
   const long long plane = (long long)nx * ny;
   Z = (int)(n / plane);

@@ -33,6 +33,7 @@ struct LbmView {
   uint32_t* ntag;                // per node: stamp of the last step whose stencils touch it
   T* unode;                      // [3][N] velocity of tagged nodes
   uint32_t* stamp;               // device step stamp (advanced by interp_advance)
+  int reverse;                   // sweep the lattice from the last z-plane down
   T omega;
   T uw[MAX_WALL_CLASSES][3];
 };
@@ -47,6 +48,16 @@ struct TypeDev {
   const int* ring;        // nv*6
   const int* ring_n;      // nv
   const int* inner;       // ni*2
+  const int* vface;       // nv*6 per-vertex adjacency (see hc_host.h)
+  const int* vedge;       // nv*6
+  const int* vopp;        // nv*6
+  const int* vinner_off;  // nv+1
+  const int* vinner;
+  const int* slot_rot;    // nv*6
+  const double* slot_a0;  // nv*6
+  const double* slot_l0;  // nv*6
+  const float* slot_a0f;
+  const float* slot_l0f;
   const double* tri_a0;
   const double* edge_l0;
   const double* edge_angle0;
@@ -89,6 +100,12 @@ struct MechView {
   const TypeDev* types;
   VertexView<T> vv;
   int dyn_smem;       // bytes available per CTA
+  // fused spread of the next step: the vertex-centric kernel spreads each
+  // new vertex force (FORCE_LIMIT-clamped) into L.Fcur and tags the stencil
+  // nodes, so the next step needs no spread pass
+  int fuse_spread;
+  LbmView<T> L;
+  T f_limit;
 };
 
 // Launch wrappers; each enqueues on `s` and returns the launch error code.
@@ -125,7 +142,7 @@ template <typename T>
 cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg,
                                   int do_interp, int do_advance, int bs, cudaStream_t s);
 template <typename T>
-cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, cudaStream_t s);
+cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, int variant, cudaStream_t s);
 template <typename T>
 size_t mechanics_smem_bytes(int nv);
 template <typename T>

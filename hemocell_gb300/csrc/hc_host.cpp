@@ -282,6 +282,46 @@ std::string build_constants(TypeConstants& tc, int model, const std::vector<Vec3
       tc.ring[6 * v + n] = cur;
     }
   }
+  // per-vertex adjacency (slot j: ring neighbour ring[j], face (i, r_j, r_j+1))
+  {
+    std::unordered_map<uint64_t, int> eid;
+    for (int e = 0; e < tc.ne; ++e) eid[key(tc.edges[2 * e], tc.edges[2 * e + 1])] = e;
+    auto edge_of = [&](int a, int b) { return eid.at(a < b ? key(a, b) : key(b, a)); };
+    tc.vface.assign(6 * tc.nv, -1);
+    tc.vedge.assign(6 * tc.nv, -1);
+    tc.vopp.assign(6 * tc.nv, -1);
+    for (int v = 0; v < tc.nv; ++v) {
+      const int rn = tc.ring_n[v];
+      for (int j = 0; j < rn; ++j) {
+        const int r = tc.ring[6 * v + j], r1 = tc.ring[6 * v + (j + 1) % rn];
+        tc.vface[6 * v + j] = dir.at(key(v, r));
+        tc.vedge[6 * v + j] = edge_of(v, r);
+        tc.vopp[6 * v + j] = edge_of(r, r1);
+      }
+    }
+    tc.slot_rot.assign(6 * tc.nv, 0);
+    tc.slot_a0.assign(6 * tc.nv, 0.0);
+    tc.slot_l0.assign(6 * tc.nv, 0.0);
+    for (int v = 0; v < tc.nv; ++v)
+      for (int j = 0; j < tc.ring_n[v]; ++j) {
+        const int k = tc.vface[6 * v + j];
+        tc.slot_rot[6 * v + j] = tris[k][0] == v ? 0 : (tris[k][1] == v ? 1 : 2);
+        tc.slot_a0[6 * v + j] = tc.tri_a0[k];
+        tc.slot_l0[6 * v + j] = tc.edge_l0[tc.vedge[6 * v + j]];
+      }
+    tc.vinner_off.assign(tc.nv + 1, 0);
+    for (int e = 0; e < tc.ni; ++e) {
+      tc.vinner_off[tc.inner[2 * e] + 1]++;
+      tc.vinner_off[tc.inner[2 * e + 1] + 1]++;
+    }
+    for (int v = 0; v < tc.nv; ++v) tc.vinner_off[v + 1] += tc.vinner_off[v];
+    tc.vinner.assign(tc.vinner_off[tc.nv], -1);
+    std::vector<int> fill(tc.vinner_off.begin(), tc.vinner_off.end() - 1);
+    for (int e = 0; e < tc.ni; ++e) {
+      tc.vinner[fill[tc.inner[2 * e]]++] = e;
+      tc.vinner[fill[tc.inner[2 * e + 1]]++] = e;
+    }
+  }
   // surface patch centre distance (commonCellConstants.cpp:284-314)
   for (int i = 0; i < tc.nv; ++i) {
     const int rn = tc.ring_n[i];

@@ -28,6 +28,16 @@ struct TypeConstants {
   std::vector<int> ring;        // nv*6 sorted 1-ring (-1 padded)
   std::vector<int> ring_n;      // nv
   std::vector<int> inner;       // ni*2
+  // per-vertex adjacency for the vertex-centric force assembly, slot j of
+  // vertex i refers to its ring neighbour ring[i][j]:
+  std::vector<int> vface;       // nv*6 triangle (i, ring[j], ring[j+1])
+  std::vector<int> vedge;       // nv*6 edge (i, ring[j])
+  std::vector<int> vopp;        // nv*6 edge (ring[j], ring[j+1]) opposite to i
+  std::vector<int> vinner_off;  // nv+1 CSR of the inner links touching i
+  std::vector<int> vinner;      // inner link ids
+  std::vector<int> slot_rot;       // nv*6 position of i in tris[vface] (0..2)
+  std::vector<double> slot_a0;     // nv*6 rest area of vface
+  std::vector<double> slot_l0;     // nv*6 rest length of vedge
   std::vector<double> tri_a0, edge_l0, edge_angle0, patch_d0, inner_l0;
   double volume_eq = 0, area_mean_eq = 0, edge_mean_eq = 0, angle_mean_eq = 0;
   std::vector<Vec3> rest;       // template vertices (lattice units)

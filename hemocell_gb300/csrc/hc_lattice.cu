@@ -17,19 +17,36 @@ namespace hcd {
 // the even and odd parts of equilibrium and Guo source:
 //   f*_{+c} = (1-w) f_{+c} + P + Q,   f*_{-c} = (1-w) f_{-c} + P - Q
 // with rho u = sum c f + F/2 (Guo, Zheng & Shi 2002).
-template <typename T>
+// ROWS: the block spans whole x-rows and pulls through shared memory
+// (pull_rows); otherwise each thread pulls directly from global memory.
+// The sweep direction alternates every step (L.reverse): a pass then starts
+// on the planes the previous pass wrote last, which are still in L2.
+template <typename T, bool ROWS>
 __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
+  extern __shared__ double k1_smem[];
   const int X = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int Z = blockIdx.z;
-  if (X >= L.nx || Y >= L.ny) return;
+  const int Z = L.reverse ? L.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
   const long long N = L.N;
-  const long long n = (long long)X + (long long)L.nx * ((long long)Y + (long long)L.ny * Z);
-  const uint32_t m = __ldg(L.nbmask + n);
-  if (m & NB_SOLID) return;
-
   T f[19];
-  pull(L, L.fsrc, X, Y, Z, n, m, f);
+  long long n;
+  uint32_t m;
+  if (ROWS) {
+    const bool inside = Y < L.ny;
+    n = (long long)X + (long long)L.nx * ((long long)(inside ? Y : 0) + (long long)L.ny * Z);
+    m = inside ? __ldg(L.nbmask + n) : NB_SOLID;
+    const bool need = !(m & NB_SOLID);
+    T* buf = reinterpret_cast<T*>(k1_smem);
+    uint32_t* msk = reinterpret_cast<uint32_t*>(buf + 10 * blockDim.y * L.nx);
+    pull_rows(L, L.fsrc, X, inside ? Y : 0, Z, n, m, need, buf, msk, f);
+    if (!need) return;
+  } else {
+    if (X >= L.nx || Y >= L.ny) return;
+    n = (long long)X + (long long)L.nx * ((long long)Y + (long long)L.ny * Z);
+    m = __ldg(L.nbmask + n);
+    if (m & NB_SOLID) return;
+    pull(L, L.fsrc, X, Y, Z, n, m, f);
+  }
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
 
@@ -73,13 +90,22 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
   FieldLayout<T>::store(L.Fnext, N, n, L.bodyz[Z], L.bodyz[L.nz + Z], L.bodyz[2 * L.nz + Z]);
 }
 
+// bx == 0 selects the row-staged kernel with blocks of (nx, by) when nx
+// allows it (nx * by <= 256); otherwise (bx, by) blocks pull directly.
 template <typename T>
 cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s) {
-  if (bx <= 0) bx = 64;
   if (by <= 0) by = 4;
+  if (bx == 0 && L.nx <= 256) {
+    while (L.nx * by > 256 && by > 1) by /= 2;
+    dim3 block(L.nx, by, 1);
+    dim3 grid(1, (L.ny + by - 1) / by, L.nz);
+    k_collide_stream<T, true><<<grid, block, pull_rows_smem<T>(L.nx, by), s>>>(L);
+    return cudaGetLastError();
+  }
+  if (bx <= 0) bx = 64;
   dim3 block(bx, by, 1);
   dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
-  k_collide_stream<T><<<grid, block, 0, s>>>(L);
+  k_collide_stream<T, false><<<grid, block, 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -90,8 +116,9 @@ cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStrea
 // L.Fcur the force of that collision.
 template <typename T>
 __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= L.N) return;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.N) return;
+  const long long n = L.reverse ? L.N - 1 - g : g;
   if (L.ntag[n] != *L.stamp) return;
   const uint32_t m = L.nbmask[n];
   int X, Y, Z;

@@ -484,6 +484,22 @@ void advance(orc_sim* s) {
 
 // --- constitutive models --------------------------------------------------
 // rbcHighOrderModel.cpp:38-207 (model 0) and wbcHighOrderModel.cpp:42-225 (model 2)
+// The volume is the reference's six-term triple-product sum
+// (rbcHighOrderModel.cpp:62-68) evaluated on coordinates relative to the
+// cell's vertex 0: a closed surface's signed volume does not depend on the
+// origin, and on absolute coordinates the sum cancels by orders of magnitude
+// (a platelet 30 lu from the origin loses ~13 digits).
+inline double faceVolume6(V3 o, V3 p0, V3 p1, V3 p2) {
+  const V3 v0 = p0 - o, v1 = p1 - o, v2 = p2 - o;
+  const double v210 = v2.x * v1.y * v0.z;
+  const double v120 = v1.x * v2.y * v0.z;
+  const double v201 = v2.x * v0.y * v1.z;
+  const double v021 = v0.x * v2.y * v1.z;
+  const double v102 = v1.x * v0.y * v2.z;
+  const double v012 = v0.x * v1.y * v2.z;
+  return (-v210 + v120 + v201 - v021 - v102 + v012);
+}
+
 void mechanicsHighOrder(orc_sim* s, const CellType& t, const Cell& c) {
   V3* X = &s->x[c.voff];
   V3* Vv = &s->v[c.voff];
@@ -496,13 +512,7 @@ void mechanicsHighOrder(orc_sim* s, const CellType& t, const Cell& c) {
   int tn = 0;
   for (const auto& tr : t.tris) {
     const V3 v0 = X[tr[0]], v1 = X[tr[1]], v2 = X[tr[2]];
-    const double v210 = v2.x * v1.y * v0.z;
-    const double v120 = v1.x * v2.y * v0.z;
-    const double v201 = v2.x * v0.y * v1.z;
-    const double v021 = v0.x * v2.y * v1.z;
-    const double v102 = v1.x * v0.y * v2.z;
-    const double v012 = v0.x * v1.y * v2.z;
-    volume += (-v210 + v120 + v201 - v021 - v102 + v012);
+    volume += faceVolume6(X[0], v0, v1, v2);
     double area;
     V3 nrm;
     areaAndUnitNormal(v0, v1, v2, area, nrm);
@@ -606,13 +616,7 @@ void mechanicsPlt(orc_sim* s, const CellType& t, const Cell& c) {
   int tn = 0;
   for (const auto& tr : t.tris) {
     const V3 v0 = X[tr[0]], v1 = X[tr[1]], v2 = X[tr[2]];
-    const double v210 = v2.x * v1.y * v0.z;
-    const double v120 = v1.x * v2.y * v0.z;
-    const double v201 = v2.x * v0.y * v1.z;
-    const double v021 = v0.x * v2.y * v1.z;
-    const double v102 = v1.x * v0.y * v2.z;
-    const double v012 = v0.x * v1.y * v2.z;
-    volume += (-v210 + v120 + v201 - v021 - v102 + v012);
+    volume += faceVolume6(X[0], v0, v1, v2);
     double area;
     V3 nrm;
     areaAndUnitNormal(v0, v1, v2, area, nrm);
@@ -899,11 +903,8 @@ void orc_read_cells(orc_sim* s, int* alive, double* volume) {
     if (volume) {
       const CellType& t = s->types[c.type];
       double vol = 0;
-      for (const auto& tr : t.tris) {
-        const V3 v0 = s->x[c.voff + tr[0]], v1 = s->x[c.voff + tr[1]], v2 = s->x[c.voff + tr[2]];
-        vol += (-v2.x * v1.y * v0.z + v1.x * v2.y * v0.z + v2.x * v0.y * v1.z - v0.x * v2.y * v1.z -
-                v1.x * v0.y * v2.z + v0.x * v1.y * v2.z);
-      }
+      for (const auto& tr : t.tris)
+        vol += faceVolume6(s->x[c.voff], s->x[c.voff + tr[0]], s->x[c.voff + tr[1]], s->x[c.voff + tr[2]]);
       volume[ci] = vol / 6.0;
     }
   }

@@ -167,11 +167,17 @@ def test_advance_and_bins_bit_exact(built):
     hc.close()
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("types", [[0], [1], [2], [0, 1, 2]])
-def test_mechanics_stage(built, types):
+def test_mechanics_stage(built, types, variant):
+    """Both force-assembly variants (0 vertex gather, 1 face/edge scatter)
+    against the oracle's face/edge/vertex loops."""
     case = mixed_box()
     case.cells = [c for c in case.cells if c[0] in types]
     hc = case.build()
+    t = hc.tuning()
+    t[6] = variant
+    hc.set_tuning(t)
     o = _orc().apply_case(case)
     randomize(case, hc, o, xamp=0.08)
     hc.stage(5)
@@ -180,25 +186,10 @@ def test_mechanics_stage(built, types):
     _, _, fo = o.read_vertices()
     assert np.abs(fo).max() > 0
     assert rel_l2(fg, fo) < STAGE_TOL
-    hc.close()
-
-
-def test_full_step_shear_rbc(built):
-    C = _cases()
-    case = C.shear_single_rbc(n=24, shear_rate=20000.0, seed=7, min_triangles=320)
-    hc = case.build()
-    o = _orc().apply_case(case)
-    hc.iterate(300)
-    o.step(300)
-    xg, vg, fg = hc.read_vertices()
-    xo, vo, fo = o.read_vertices()
-    rg, ug = hc.read_fluid()
-    ro, uo = o.read_fluid()
-    assert rel_l2(xg, xo) < RUN_TOL
-    assert rel_l2(vg, vo) < RUN_TOL
-    assert rel_l2(fg, fo) < 1e-8
-    assert rel_l2(ug, uo) < RUN_TOL
-    assert rel_l2(rg, ro) < RUN_TOL
+    if variant == 0:  # no atomics: the same inputs give the same bits
+        hc.stage(5)
+        _, _, fg2 = hc.read_vertices()
+        assert np.array_equal(fg, fg2)
     hc.close()
 
 
@@ -258,6 +249,37 @@ def test_full_step_mixed_types_batched_graph(built):
 
 def o_iter(o):
     return o.L.orc_iter(o.s)
+
+
+def test_batched_state_changes_between_steps(built):
+    """The batched form spreads the next step's forces inside the membrane
+    kernel; host-side changes between steps (vertex rewrite, body force,
+    timescales) must fall back to the standalone spread and stay exact."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_periodic()
+    o = _orc().apply_case(case)
+    hb = case.build(launch=L.HC_LAUNCH_BATCHED)
+    hb.iterate(20)
+    o.step(20)
+    x, v, f = o.read_vertices()
+    hb.write_vertices(x, v, f)
+    o.write_vertices(x, v, f)
+    hb.setExternalVector(case.body_mode, case.body)
+    o.set_body_force(case.body_mode, case.body)
+    hb.iterate(21)
+    o.step(21)
+    hb.setMaterialTimeScaleSeparation([2, 2, 2], velocity_every=1)
+    o.set_timescales([2, 2, 2], 1)
+    hb.iterate(10)
+    o.step(10)
+    xg, vg, _ = hb.read_vertices()
+    xo, vo, _ = o.read_vertices()
+    assert rel_l2(xg, xo) < RUN_TOL
+    assert rel_l2(vg, vo) < RUN_TOL
+    _, ug = hb.read_fluid()
+    _, uo = o.read_fluid()
+    assert rel_l2(ug, uo) < RUN_TOL
+    hb.close()
 
 
 def test_timescale_separation(built):
