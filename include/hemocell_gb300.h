@@ -180,7 +180,7 @@ int hc_mesh_antipodal_pairs(const double* xyz, int nv, int* pairs, int max_pairs
  * rad) and translated; out_xyz holds n*nv*3 doubles */
 int hc_place_cells(const double* template_xyz, int nv, int n, const double* centres, const double* angles,
                    double* out_xyz);
-/* seeded non-overlapping packing of cells (see DESIGN: replaces tools/packCells):
+/* seeded non-overlapping packing of cells (stands in for the reference's packCells tool):
  * type_xyz/type_nv/type_tris/type_nf describe ntypes rest shapes, counts[t]
  * cells per type; solid[N] marks forbidden nodes (may be NULL); margin in
  * lattice units.  Writes centres[total*3], angles[total*3], types[total];
