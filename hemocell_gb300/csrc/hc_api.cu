@@ -827,6 +827,8 @@ int restore_populations(hc_handle* h, const std::function<int()>& change) {
 
 }  // namespace
 
+void hcd::set_handleless_error(const std::string& msg) { g_create_error = msg; }
+
 // ===========================================================================
 extern "C" {
 

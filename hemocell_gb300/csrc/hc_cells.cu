@@ -1088,6 +1088,17 @@ cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, cons
   return cudaGetLastError();
 }
 
+cudaError_t launch_exclusive_scan(const int* in, int n, int* out, cudaStream_t s) {
+  k_scan<<<1, 1024, 0, s>>>(in, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* vcell, int ntiles,
+                             int* tile_cell_counts, cudaStream_t s) {
+  k_bin_sort<<<ntiles, 256, 0, s>>>(offsets, tile_vertices, vcell, tile_cell_counts);
+  return cudaGetLastError();
+}
+
 #define HC_CELL_INST(T)                                                                                        \
   template cudaError_t launch_spread<T>(const LbmView<T>&, const VertexView<T>&, double, int, cudaStream_t);   \
   template cudaError_t launch_mark_nodes<T>(const LbmView<T>&, const VertexView<T>&, cudaStream_t);            \

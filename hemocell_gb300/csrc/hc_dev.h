@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 namespace hcd {
 
 constexpr uint32_t NB_SOLID = 1u << 23;  // node itself is a wall node
@@ -157,5 +159,13 @@ cudaError_t launch_bin_csr(const int* vtile, int nvert, int ntiles, int* counts,
 cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, const int* vcell, int ntiles,
                               int* tile_cell_counts, int* tile_cell_offsets, int* tile_cells, int max_cells,
                               cudaStream_t s);
+// the two middle steps of the tile CSR on their own: out[0..n] = exclusive
+// scan of in[0..n-1]; per-tile sort of tile_vertices and distinct cells per tile
+cudaError_t launch_exclusive_scan(const int* in, int n, int* out, cudaStream_t s);
+cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* vcell, int ntiles,
+                             int* tile_cell_counts, cudaStream_t s);
+
+// message returned by hc_last_error(NULL) for calls that take no handle
+void set_handleless_error(const std::string& msg);
 
 }  // namespace hcd

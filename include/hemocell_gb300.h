@@ -90,7 +90,9 @@ typedef struct hc_stats {
 /* --- lifecycle: HemoCell::HemoCell / ~HemoCell (core/hemoCell.cpp:69-127) */
 hc_handle* hc_create(const hc_params* p);
 int hc_destroy(hc_handle* h);
-const char* hc_last_error(const hc_handle* h); /* h may be NULL: last create error */
+const char* hc_last_error(const hc_handle* h); /* h may be NULL: last failure of a call
+                                                  without a handle (hc_create,
+                                                  hc_bin_tiles_noalloc) */
 /* Parameters::lbm_base_parameters (mechanics/constantConversion.cpp:36-59):
  * out = {tau, nu_lbm, dm, df, kBT_lbm, f_limit} */
 int hc_derived_units(const hc_handle* h, double* out6);
@@ -153,6 +155,33 @@ int hc_read_cells(hc_handle* h, int* alive, double* volume);
  * tile_cell_offsets[ntiles+1], tile_cells[max_tile_cells].  Returns ntiles. */
 int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_offsets,
                  int* tile_vertices, int* tile_cell_offsets, int* tile_cells, int max_tile_cells);
+/* Tile binning that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that must not have a library allocate on
+ * their behalf -- a program whose device memory is already carved up by its
+ * own pool allocator, or host code on a latency-critical thread that cannot
+ * pay for cudaMalloc/cudaFree, which may synchronise the device.  It builds
+ * the same lists as hc_read_bins from device-resident inputs, without a handle.
+ *
+ * All pointers are DEVICE pointers on the current device; work is enqueued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and the call returns
+ * without waiting for it.  Inputs: vertex_tile[nvert] (tile of each vertex,
+ * -1 or any value outside [0, ntiles) = not binned), vertex_cell[nvert].
+ * Outputs: tile_offsets[ntiles+1], tile_vertices[nvert] (ascending within a
+ * tile), tile_cell_offsets[ntiles+1], tile_cells[max_tile_cells] (cells per
+ * tile in ascending order; if tile_cell_offsets[ntiles] > max_tile_cells the
+ * list is cut at max_tile_cells).
+ *
+ * Limit: ntiles <= 131072; larger requests return HC_ERR_INVALID with the
+ * reason in hc_last_error(NULL).  The per-tile counters live in one fixed
+ * 1.5 MiB array in the library's device memory, shared by every call on a
+ * device: calls that may run concurrently (two host threads, or unordered
+ * streams) race on it and give wrong lists; calls ordered on one stream are
+ * safe.  The first call on each device looks up that array's address (with
+ * the device current), which may make the CUDA runtime load the library's
+ * device code; make that first call before capturing any stream. */
+int hc_bin_tiles_noalloc(const int* vertex_tile, const int* vertex_cell, int nvert, int ntiles,
+                         int* tile_offsets, int* tile_vertices, int* tile_cell_offsets, int* tile_cells,
+                         int max_tile_cells, void* stream);
 int hc_get_stats(hc_handle* h, hc_stats* out);
 /* last device status word: bit0 non-finite vertex velocity, bit1 cell deleted at a wall */
 int hc_device_status(hc_handle* h, unsigned int* status);
