@@ -20,9 +20,14 @@ FP32, ~370 MB in FP64) exceeds the 129 MB L2, so no flush is inserted.
 """
 from __future__ import annotations
 
+import os
+
+# the serving leg runs up to 64 solves on their own streams: give the device
+# enough hardware queues that they do not serialise (read at context creation)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 import argparse
 import json
-import os
 import statistics
 import subprocess
 import sys
@@ -37,9 +42,10 @@ sys.path.insert(0, ROOT)
 # algorithmic bytes per fluid node and per vertex of one step
 BYTES_NODE = {"f32": 2 * 19 * 4 + 2 * 3 * 4, "f64": 2 * 19 * 8 + 2 * 3 * 8}
 BYTES_VERTEX = {"f32": 2 * 3 * 8 + 2 * 2 * 3 * 4, "f64": 2 * 3 * 3 * 8}
-# DRAM bytes per fluid node of the collide-stream kernel, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum on the 64x64x256 pipe)
-K1_TRAFFIC_PER_NODE = {"f32": None, "f64": None}
+# DRAM bytes of one collide-stream launch on this workload, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, --set full capture of the
+# 64x64x256 pipe with 279 RBC; the summary is in profiles/)
+K1_TRAFFIC_PER_LAUNCH = {"f32": 105.014784e6 + 33.601536e6, "f64": 174.845696e6 + 93.809152e6}
 
 
 def measured_peaks():
@@ -163,6 +169,119 @@ def cpu_baseline(case, budget_s: float = 12.0, threads: int = 0):
     return case.N * n / dt / 1e6, n, threads
 
 
+def max_over_ranks(x: float) -> float:
+    """Largest x over the ranks of the process group (x itself without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_mlups(world: int, nodes: int, steps: int, ms_max: float) -> float:
+    """Whole-job MLUPS of `world` independent replicas timed by the slowest."""
+    return world * nodes * steps / (ms_max * 1e3)
+
+
+def rel_l2(a, b) -> float:
+    d = np.linalg.norm(np.asarray(a, np.float64) - np.asarray(b, np.float64))
+    n = np.linalg.norm(np.asarray(b, np.float64))
+    return float(d / n) if n > 0 else float(d)
+
+
+def mixed_error_leg(case, steps: int = 2000, every: int = 100):
+    """The mixed FP32 form against the FP64 plain form (which matches the FP64
+    oracle within 1e-10) on the same workload: velocity and density relative
+    L2 over the fluid, and per-cell volume difference, every `every` steps."""
+    from hemocell_gb300 import _lib as L
+    a = case.build(form=L.HC_FORM_MIXED_F32, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=L.HC_FORM_PLAIN_F64, launch=L.HC_LAUNCH_BATCHED)
+    fluid = case.flags_array() == 0
+    _, v0 = b.read_cells()
+    rec = {"steps": [], "u_rel_l2": [], "rho_rel_l2": [], "volume_rel_max": [], "volume_drift_f32": [],
+           "volume_drift_f64": []}
+    for k in range(every, steps + 1, every):
+        a.iterate(every)
+        b.iterate(every)
+        ra, ua = a.read_fluid()
+        rb, ub = b.read_fluid()
+        _, va = a.read_cells()
+        _, vb = b.read_cells()
+        rec["steps"].append(k)
+        rec["u_rel_l2"].append(rel_l2(ua[:, fluid], ub[:, fluid]))
+        rec["rho_rel_l2"].append(rel_l2(ra[fluid], rb[fluid]))
+        rec["volume_rel_max"].append(float(np.max(np.abs(va - vb) / v0)))
+        rec["volume_drift_f32"].append(float(np.max(np.abs(va - v0) / v0)))
+        rec["volume_drift_f64"].append(float(np.max(np.abs(vb - v0) / v0)))
+    a.close()
+    b.close()
+    return rec
+
+
+def kolmogorov_leg(steps: int, warmup: int, tune_cache):
+    """128^3 periodic cube, Kolmogorov forcing, 30% RBC volume fraction with
+    platelets (1 per 10 RBC) and 2 WBC: MLUPS of both forms, batched."""
+    from hemocell_gb300 import _lib as L
+    from hemocell_gb300 import cases
+    t0 = time.perf_counter()
+    case = cases.kolmogorov_mix(n=128, seed=1)
+    pack_s = time.perf_counter() - t0
+    out = {"workload": "kolmogorov_128: 128^3 periodic, F_x = A sin(2 pi z/128), 30% RBC (642 vertices), "
+                       "PLT (162 vertices) 1 per 10 RBC, 2 WBC (2562 vertices)",
+           "cells": len(case.cells), "vertices": case.nvertices, "packing_s": pack_s}
+    for name, form in (("fp32_batched", L.HC_FORM_MIXED_F32), ("fp64_batched", L.HC_FORM_PLAIN_F64)):
+        ms, prof, clocks, st, status, tuning = time_form(case, form, L.HC_LAUNCH_BATCHED, steps, warmup,
+                                                         tune_cache)
+        out[name] = {"value": case.N * steps / (ms * 1e3), "unit": "MLUPS", "ms_per_step": ms / steps,
+                     "stages_ms": prof, "tuning": tuning, "status": status, "clocks": clocks}
+    out["fp32_over_fp64"] = out["fp32_batched"]["value"] / out["fp64_batched"]["value"]
+    return out
+
+
+def serving_leg(args):
+    """Continuous batching of the stream of independent sheared-box solves
+    (box edge 32-96, 1-8 RBC, 500-5000 steps, Poisson arrivals at 200/s):
+    solves/s and latency of the batched server in FP32 and FP64, against the
+    same requests run one at a time in the plain FP64 form."""
+    import torch
+    from hemocell_gb300 import _lib as L
+    from hemocell_gb300 import serving as S
+    stream = S.request_stream(seed=1, rate=200.0, count=10000)
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(min(0.5 * free, 64 << 30))
+    head = stream[:args.serve_requests]
+    few = stream[:args.serve_solo]
+    solves = {r.id: S.Solve(r) for r in head}        # geometry and packing, outside the clock
+    kw = dict(budget_bytes=budget, max_slots=64, chunk_steps=50, solves=solves)
+
+    def trim(d):
+        return {k: v for k, v in d.items() if k != "results"}
+
+    solo = S.solo(few, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_PER_STAGE, solves=solves)
+    few32 = S.serve(few, L.HC_FORM_MIXED_F32, **kw)
+    few64 = S.serve(few, L.HC_FORM_PLAIN_F64, **kw)
+    sat32 = S.serve(head, L.HC_FORM_MIXED_F32, **kw)
+    # below saturation: the same requests at half the measured FP32 capacity
+    rate_sub = 0.5 * sat32["solves_per_s"]
+    sub = S.with_arrivals(head[: max(8, args.serve_requests // 3)], rate_sub, seed=2)
+    sub32 = S.serve(sub, L.HC_FORM_MIXED_F32, **kw)
+    return {
+        "workload": "independent sheared boxes, edge U{32,48,64,96}, 1-8 RBC (642 vertices), shear 50-500/s, "
+                    "kLink/kBend x log-U(0.5,5), 500-5000 steps; Poisson arrivals, seed 1",
+        "budget_bytes": budget, "max_slots": 64, "chunk_steps": 50,
+        "solo_plain_f64": trim(solo),
+        "batched_f32_same_requests": trim(few32),
+        "batched_f64_same_requests": trim(few64),
+        "speedup_f32_vs_solo": few32["solves_per_s"] / solo["solves_per_s"],
+        "speedup_f64_vs_solo": few64["solves_per_s"] / solo["solves_per_s"],
+        "saturated_f32_200_per_s": trim(sat32),
+        "subsaturated_f32": dict(trim(sub32), offered_rate_target=rate_sub),
+    }
+
+
 def run_reference(args):
     """--impl reference: the CPU restatement of the reference path, all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -198,12 +317,18 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain form")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-stream leg")
+    ap.add_argument("--no-kolmogorov", action="store_true", help="skip the 128^3 suspension leg")
+    ap.add_argument("--no-mixed-error", action="store_true", help="skip the FP32-vs-FP64 error report")
+    ap.add_argument("--serve-requests", type=int, default=96, help="requests of the saturated FP32 stream")
+    ap.add_argument("--serve-solo", type=int, default=12, help="requests run one at a time (and batched) "
+                                                                 "for the speed-up")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -229,17 +354,13 @@ def main():
         torch.distributed.barrier()
     ms, prof, clocks, st, status, tuning = time_form(case, L.HC_FORM_MIXED_F32, L.HC_LAUNCH_BATCHED, args.steps,
                                                      args.warmup, tune_cache)
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * case.N * args.steps / (ms_max * 1e3)
+    ms_max = max_over_ranks(ms)
+    value = replicas_mlups(world, case.N, args.steps, ms_max)
     peak, peak_kind = measured_peaks()
     k1_ms = prof["collide_stream"]
     k1_bytes = fluid * BYTES_NODE["f32"]
     achieved = k1_bytes / (k1_ms * 1e-3) / 1e9
-    traffic = None if K1_TRAFFIC_PER_NODE["f32"] is None else K1_TRAFFIC_PER_NODE["f32"] * fluid
+    traffic = K1_TRAFFIC_PER_LAUNCH["f32"]
     step_bytes = fluid * BYTES_NODE["f32"] + st.vertices * BYTES_VERTEX["f32"]
     step_gbs = step_bytes / (ms / args.steps * 1e-3) / 1e9
 
@@ -256,6 +377,13 @@ def main():
                                 args.warmup)
     e2e_steps = max(20, args.steps // 4)
     e2e_val = world * case.N * e2e_steps / e2e_dt / 1e6
+
+    if not args.no_mixed_error:
+        extra["mixed_vs_fp64"] = mixed_error_leg(case)
+    if not args.no_kolmogorov:
+        extra["kolmogorov"] = kolmogorov_leg(min(args.steps, 1000), args.warmup, tune_cache)
+    if not args.no_serving:
+        extra["serving"] = serving_leg(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -55,6 +55,12 @@ class hc_stats(C.Structure):
                 ("device_bytes", C.c_longlong)]
 
 
+class hc_batch_stats(C.Structure):
+    _fields_ = [("active", C.c_int), ("finished", C.c_int), ("popped", C.c_int), ("max_slots", C.c_int),
+                ("budget_bytes", C.c_longlong), ("bytes_in_use", C.c_longlong), ("admitted", C.c_longlong),
+                ("completed", C.c_longlong), ("refused", C.c_longlong), ("steps_enqueued", C.c_longlong)]
+
+
 P = C.c_void_p
 D = C.POINTER(C.c_double)
 I = C.POINTER(C.c_int)
@@ -103,6 +109,16 @@ SIGNATURES = {
     "hc_place_cells": (C.c_int, [D, C.c_int, C.c_int, D, D, D]),
     "hc_pack_cells": (C.c_int, [C.c_int, C.c_int, C.c_int, I, U8, C.c_int, C.POINTER(D), I, C.POINTER(I), I, I,
                                 C.c_double, C.c_ulonglong, C.c_int, D, D, I]),
+    "hc_estimate_device_bytes": (C.c_longlong, [C.POINTER(hc_params), C.c_int, C.c_int]),
+    "hc_batch_create": (P, [C.c_int, C.c_longlong, C.c_int, C.c_int]),
+    "hc_batch_destroy": (C.c_int, [P]),
+    "hc_batch_last_error": (C.c_char_p, [P]),
+    "hc_batch_fits": (C.c_int, [P, C.c_longlong]),
+    "hc_batch_admit": (C.c_int, [P, P, C.c_int, C.c_longlong]),
+    "hc_batch_pump": (C.c_int, [P, C.c_double]),
+    "hc_batch_pop": (C.c_int, [P, C.POINTER(C.c_longlong), C.POINTER(P), I]),
+    "hc_batch_release": (C.c_int, [P, P, C.c_int]),
+    "hc_batch_get_stats": (C.c_int, [P, C.POINTER(hc_batch_stats)]),
 }
 
 _lib = None

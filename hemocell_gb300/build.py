@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhcgpu.so")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
-UNITS = ["hc_lattice.cu", "hc_cells.cu", "hc_api.cu", "hc_noalloc.cu", "hc_host.cpp"]
+UNITS = ["hc_lattice.cu", "hc_cells.cu", "hc_api.cu", "hc_noalloc.cu", "hc_batch.cu", "hc_host.cpp"]
 
 
 def _nvcc() -> str:

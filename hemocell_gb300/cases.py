@@ -203,6 +203,28 @@ def kolmogorov_mix(n: int = 128, rbc_fraction: float = 0.30, n_wbc: int = 2, plt
                 types=types, cells=cells, steps=steps)
 
 
+def mixed_box(seed: int = 5, n: Tuple[int, int, int] = (20, 18, 16), wall: bool = True) -> Case:
+    """Small box with one cell of each type (RBC 162, PLT 42, WBC 162 vertices)
+    and, optionally, moving walls: the stage-by-stage parity case."""
+    nx, ny, nz = n
+    if wall:
+        flags, walls = shear_walls(n, 5000.0)
+        periodic = (1, 1, 0)
+    else:
+        flags, walls, periodic = None, {}, (1, 1, 1)
+    types = [rbc_type(320), plt_type(80, radius_m=1.0e-6, aspect=0.4), wbc_type(320)]
+    rng = np.random.default_rng(seed)
+    cells = []
+    centres = [((nx - 1) / 2, (ny - 1) / 2 - 3.5, (nz - 1) / 2), ((nx - 1) / 2 + 4, (ny - 1) / 2 + 5, (nz - 1) / 2),
+               ((nx - 1) / 2 - 4.5, (ny - 1) / 2 + 4.0, (nz - 1) / 2 + 1)]
+    for t, c in enumerate(centres):
+        ang = rng.uniform(-np.pi, np.pi, size=(1, 3))
+        xyz = place_cells(types[t].mesh, np.array([c]), ang)
+        cells.append((t, xyz))
+    return Case("mixed_box", n, periodic, flags=flags, walls=walls, types=types, cells=cells,
+                body_mode=1, body=(2e-6, -1e-6, 5e-7))
+
+
 def stretch_cell(min_triangles: int = 600) -> Case:
     """Single RBC in a closed 52x26x26 box (tests/validation/stretch_cell):
     nuP 1.1e-6, dt 1e-7 -> tau 1.82; box faces are static walls; the cell is

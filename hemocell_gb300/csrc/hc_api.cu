@@ -8,11 +8,13 @@
 #include <fstream>
 #include <functional>
 #include <map>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
 
 #include "../../include/hemocell_gb300.h"
+#include "hc_d3q19.cuh"
 #include "hc_dev.h"
 #include "hc_host.h"
 
@@ -98,6 +100,7 @@ struct hc_handle {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool graph_valid = false;
   long long device_bytes = 0;
+  cudaMemPool_t pool = nullptr;  // this device's library pool (all allocations)
   double* scratch = nullptr;  // readback staging
   size_t scratch_bytes = 0;
   // the spread of the coming step was already done by the last mechanics
@@ -126,14 +129,60 @@ int fail(hc_handle* h, int code, const std::string& msg) {
   return code;
 }
 
+// One stream-ordered memory pool per device holds the memory of every handle
+// on it.  Memory a handle frees stays in the pool (release threshold: never)
+// and is reused by the next handle without another cudaMalloc; the pool is
+// trimmed back to the system when the last handle on the device is destroyed.
+constexpr int kPoolDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pool[kPoolDevices] = {};
+int g_live_handles[kPoolDevices] = {};
+
+cudaError_t acquire_pool(int dev, cudaMemPool_t* out) {
+  if (dev < 0 || dev >= kPoolDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = ~0ull;
+    if ((e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return e;
+    }
+    g_pool[dev] = pool;
+  }
+  g_live_handles[dev]++;
+  *out = g_pool[dev];
+  return cudaSuccess;
+}
+
+// Called by a handle that held the pool, after its frees were enqueued.
+void release_pool(int dev, cudaStream_t s) {
+  std::lock_guard<std::mutex> lock(g_pool_mutex);
+  if (dev < 0 || dev >= kPoolDevices || g_live_handles[dev] <= 0) return;
+  if (--g_live_handles[dev] == 0 && g_pool[dev]) {
+    if (s) cudaStreamSynchronize(s);
+    cudaMemPoolTrimTo(g_pool[dev], 0);
+  }
+}
+
 cudaError_t dalloc(hc_handle* h, void** p, size_t bytes) {
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaError_t e = cudaMallocFromPoolAsync(p, bytes, h->pool, h->stream);
   if (e == cudaSuccess) h->device_bytes += (long long)bytes;
   return e;
 }
 
-void dfree(void* p) {
-  if (p) cudaFree(p);
+// Returns memory to the pool in the order of the handle's stream: unlike
+// cudaFree it does not wait for the other streams of the device.
+void dfree(hc_handle* h, void* p) {
+  if (p) cudaFreeAsync(p, h->stream);
 }
 
 void invalidate_graph(hc_handle* h) {
@@ -167,6 +216,10 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   L.omega = (T)(1.0 / h->u.tau);
   for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
+  L.fast = 19LL * h->N < (1LL << 31) ? 1 : 0;
+  const long long nxy = (long long)h->nx * h->ny;
+  for (int j = 0; j < 19; ++j)
+    L.off[j] = L.fast ? (int)(j * h->N - (hcd::cxi(j) + hcd::cyi(j) * (long long)h->nx + hcd::czi(j) * nxy)) : 0;
   return L;
 }
 
@@ -268,7 +321,7 @@ int upload_body(hc_handle* h) {
 int ensure_scratch(hc_handle* h, size_t bytes) {
   if (h->scratch_bytes >= bytes) return HC_OK;
   if (h->scratch) {
-    cudaFree(h->scratch);
+    dfree(h, h->scratch);
     h->device_bytes -= (long long)h->scratch_bytes;
   }
   h->scratch = nullptr;
@@ -276,6 +329,18 @@ int ensure_scratch(hc_handle* h, size_t bytes) {
   HC_CUDA(h, dalloc(h, (void**)&h->scratch, bytes));
   h->scratch_bytes = bytes;
   return HC_OK;
+}
+
+// Staging larger than the steady readbacks need (hc_read_fluid: 4 doubles per
+// node) is only used by set-up and population transfers: give it back, so a
+// resident handle holds no more than hc_estimate_device_bytes counts.
+void shrink_scratch(hc_handle* h) {
+  if (h->scratch && h->scratch_bytes > sizeof(double) * 4 * (size_t)h->N) {
+    dfree(h, h->scratch);
+    h->device_bytes -= (long long)h->scratch_bytes;
+    h->scratch = nullptr;
+    h->scratch_bytes = 0;
+  }
 }
 
 // grow a [3][V] SoA array from capacity oldV to newV
@@ -289,7 +354,7 @@ int grow3(hc_handle* h, void** p, size_t es, long long oldV, long long newV, int
                                  cudaMemcpyDeviceToDevice, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   if (*p) {
-    cudaFree(*p);
+    dfree(h, *p);
     h->device_bytes -= (long long)(3 * es * oldV);
   }
   *p = np;
@@ -303,7 +368,7 @@ int grow1(hc_handle* h, void** p, size_t es, long long oldn, long long newn, lon
   if (*p && nused > 0) HC_CUDA(h, cudaMemcpyAsync(np, *p, es * nused, cudaMemcpyDeviceToDevice, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   if (*p) {
-    cudaFree(*p);
+    dfree(h, *p);
     h->device_bytes -= (long long)(es * oldn);
   }
   *p = np;
@@ -323,7 +388,7 @@ int upload_types(hc_handle* h) {
 int upload_cell_lists(hc_handle* h) {
   for (TypeSlot& ts : h->types) {
     if ((int)ts.cells.size() > ts.dcells_cap) {
-      dfree(ts.dcells);
+      dfree(h, ts.dcells);
       ts.dcells_cap = std::max<int>((int)ts.cells.size(), 2 * ts.dcells_cap);
       HC_CUDA(h, dalloc(h, (void**)&ts.dcells, sizeof(int) * ts.dcells_cap));
     }
@@ -533,8 +598,8 @@ int run_stage(hc_handle* h, int stage) {
       LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
       HC_CUDA(h, hcd::launch_bin_vertices<T>(L, vertex_view<T>(h), h->tg, h->stream));
       if (h->bin_vcap < h->Vcap || !h->bin_counts) {
-        dfree(h->tile_vertices);
-        dfree(h->tile_cells);
+        dfree(h, h->tile_vertices);
+        dfree(h, h->tile_cells);
         HC_CUDA(h, dalloc(h, (void**)&h->tile_vertices, sizeof(int) * std::max<long long>(1, h->Vcap)));
         HC_CUDA(h, dalloc(h, (void**)&h->tile_cells, sizeof(int) * std::max<long long>(1, h->Vcap)));
         h->bin_vcap = h->Vcap;
@@ -704,8 +769,8 @@ int autotune(hc_handle* h, const char* cache) {
   const size_t vb = 3 * h->ts * (size_t)h->Vcap;
   void *sv = nullptr, *sf = nullptr;
   if (h->Vcap > 0) {
-    HC_CUDA(h, cudaMalloc(&sv, vb));
-    HC_CUDA(h, cudaMalloc(&sf, vb));
+    HC_CUDA(h, cudaMallocFromPoolAsync(&sv, vb, h->pool, h->stream));
+    HC_CUDA(h, cudaMallocFromPoolAsync(&sf, vb, h->pool, h->stream));
     HC_CUDA(h, cudaMemcpyAsync(sv, h->v, vb, cudaMemcpyDeviceToDevice, h->stream));
     HC_CUDA(h, cudaMemcpyAsync(sf, h->fv, vb, cudaMemcpyDeviceToDevice, h->stream));
   }
@@ -766,8 +831,8 @@ int autotune(hc_handle* h, const char* cache) {
     HC_CUDA(h, cudaMemcpyAsync(h->fv, sf, vb, cudaMemcpyDeviceToDevice, h->stream));
   }
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (sv) cudaFree(sv);
-  if (sf) cudaFree(sf);
+  dfree(h, sv);
+  dfree(h, sf);
   invalidate_graph(h);
   if (cache && *cache) {
     std::ofstream out(cache, std::ios::app);
@@ -822,12 +887,16 @@ int restore_populations(hc_handle* h, const std::function<int()>& change) {
   if (h->f64) HC_CUDA(h, hcd::launch_stream_in<double>(lbm_view<double>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
   else HC_CUDA(h, hcd::launch_stream_in<float>(lbm_view<float>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  shrink_scratch(h);
   return HC_OK;
 }
 
 }  // namespace
 
 void hcd::set_handleless_error(const std::string& msg) { g_create_error = msg; }
+cudaStream_t hcd::handle_stream(const hc_handle* h) { return h->stream; }
+int hcd::handle_device(const hc_handle* h) { return h->p.device; }
+long long hcd::handle_bytes(const hc_handle* h) { return h->device_bytes; }
 
 // ===========================================================================
 extern "C" {
@@ -890,6 +959,8 @@ hc_handle* hc_create(const hc_params* p) {
   if (e != cudaSuccess) return bail(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(std::string("stream: ") + cudaGetErrorString(e));
+  if ((e = acquire_pool(p->device, &h->pool)) != cudaSuccess)
+    return bail(std::string("memory pool: ") + cudaGetErrorString(e));
   const size_t fb = 19 * h->ts * (size_t)h->N;
   const size_t Fb = h->f64 ? hcd::field_bytes<double>(h->N) : hcd::field_bytes<float>(h->N);
   for (int k = 0; k < 2; ++k) {
@@ -925,19 +996,20 @@ int hc_destroy(hc_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   invalidate_graph(h);
   for (int k = 0; k < 2; ++k) {
-    dfree(h->f[k]);
-    dfree(h->F[k]);
+    dfree(h, h->f[k]);
+    dfree(h, h->F[k]);
   }
   for (TypeSlot& ts : h->types) {
-    dfree(ts.blob);
-    dfree(ts.dcells);
+    dfree(h, ts.blob);
+    dfree(h, ts.dcells);
   }
   void* ptrs[] = {h->ntag, h->unode, h->stamp, h->nbmask, h->flag,  h->bodyz,     h->dtypes,     h->x,          h->v,
                   h->fv,     h->vcell, h->vnode,     h->vtile,      h->cell_type,  h->cell_voff,
                   h->alive,  h->dcells_all, h->status, h->bin_counts, h->bin_cursor, h->bin_offsets,
                   h->tile_vertices, h->tile_cell_counts, h->tile_cell_offsets, h->tile_cells, h->scratch,
                   h->ext_ids, h->ext_f};
-  for (void* q : ptrs) dfree(q);
+  for (void* q : ptrs) dfree(h, q);
+  if (h->pool) release_pool(h->p.device, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return HC_OK;
@@ -1050,9 +1122,12 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
   std::vector<float> fv(dv.begin(), dv.end());
   const size_t ib = 4 * iv.size(), db = 8 * std::max<size_t>(dv.size(), 1), fb = 4 * std::max<size_t>(fv.size(), 1);
   HC_CUDA(h, dalloc(h, &ts.blob, ib + db + fb));
-  HC_CUDA(h, cudaMemcpy(ts.blob, iv.data(), ib, cudaMemcpyHostToDevice));
-  if (!dv.empty()) HC_CUDA(h, cudaMemcpy((char*)ts.blob + ib, dv.data(), 8 * dv.size(), cudaMemcpyHostToDevice));
-  if (!fv.empty()) HC_CUDA(h, cudaMemcpy((char*)ts.blob + ib + db, fv.data(), 4 * fv.size(), cudaMemcpyHostToDevice));
+  HC_CUDA(h, cudaMemcpyAsync(ts.blob, iv.data(), ib, cudaMemcpyHostToDevice, h->stream));
+  if (!dv.empty())
+    HC_CUDA(h, cudaMemcpyAsync((char*)ts.blob + ib, dv.data(), 8 * dv.size(), cudaMemcpyHostToDevice, h->stream));
+  if (!fv.empty())
+    HC_CUDA(h, cudaMemcpyAsync((char*)ts.blob + ib + db, fv.data(), 4 * fv.size(), cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
   const int* ibase = (const int*)ts.blob;
   const double* dbase = (const double*)((char*)ts.blob + ib);
   const float* fbase = (const float*)((char*)ts.blob + ib + db);
@@ -1152,8 +1227,8 @@ int hc_set_vertex_forces(hc_handle* h, int n, const int* ids, const double* forc
   for (int k = 0; k < n; ++k)
     if (ids[k] < 0 || ids[k] >= h->nvert) return fail(h, HC_ERR_INVALID, "vertex id out of range");
   if (n > h->next_cap) {
-    dfree(h->ext_ids);
-    dfree(h->ext_f);
+    dfree(h, h->ext_ids);
+    dfree(h, h->ext_f);
     h->ext_ids = nullptr;
     h->ext_f = nullptr;
     HC_CUDA(h, dalloc(h, (void**)&h->ext_ids, sizeof(int) * n));
@@ -1230,6 +1305,7 @@ int hc_read_populations(hc_handle* h, double* f) {
   else HC_CUDA(h, hcd::launch_stream_out<float>(lbm_view<float>(h, h->cur, h->cur), h->scratch, h->stream));
   HC_CUDA(h, cudaMemcpyAsync(f, h->scratch, 8 * 19 * h->N, cudaMemcpyDeviceToHost, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  shrink_scratch(h);
   return HC_OK;
 }
 
@@ -1241,6 +1317,7 @@ int hc_write_populations(hc_handle* h, const double* f) {
   if (h->f64) HC_CUDA(h, hcd::launch_stream_in<double>(lbm_view<double>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
   else HC_CUDA(h, hcd::launch_stream_in<float>(lbm_view<float>(h, 1 - h->cur, h->cur), h->scratch, 1.0, nullptr, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  shrink_scratch(h);
   return HC_OK;
 }
 
@@ -1351,6 +1428,32 @@ int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_off
     HC_CUDA(h, cudaMemcpyAsync(tile_cells, h->tile_cells, 4 * (size_t)tco[nt], cudaMemcpyDeviceToHost, h->stream));
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return nt;
+}
+
+long long hc_estimate_device_bytes(const hc_params* p, int nvertices, int ncells) {
+  if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0 || nvertices < 0 || ncells < 0) return HC_ERR_INVALID;
+  const long long N = (long long)p->nx * p->ny * p->nz;
+  const bool f64 = p->form == HC_FORM_PLAIN_F64;
+  const long long ts = f64 ? 8 : 4;
+  const long long fb = 19 * ts * N;
+  const long long Fb = (long long)(f64 ? hcd::field_bytes<double>(N) : hcd::field_bytes<float>(N));
+  // lattice arrays, as hc_create allocates them
+  long long b = 2 * fb + 2 * Fb + 4 * N + Fb + 4 + 4 * N + N + 3 * ts * p->nz +
+                (long long)sizeof(TypeDev) * hcd::MAX_TYPES + 4;
+  // vertex and cell arrays at the capacity growth can reach (twice the need)
+  const long long vcap = std::max<long long>(2LL * nvertices, 1024);
+  const long long ccap = std::max<long long>(2LL * ncells, 64);
+  b += vcap * (3 * 8 + 6 * ts + 3 * 4) + ccap * 4 * 4;
+  // per-type rest-state blobs and cell lists: at most ~512 bytes per vertex
+  b += 512LL * nvertices + 4LL * ncells;
+  // tile lists (hc_read_bins) and readback staging (hc_read_fluid, hc_read_vertices)
+  const int tx = p->tile[0] > 0 ? p->tile[0] : 8, ty = p->tile[1] > 0 ? p->tile[1] : 8,
+            tz = p->tile[2] > 0 ? p->tile[2] : 8;
+  const long long ntiles =
+      (long long)((p->nx + tx - 1) / tx) * ((p->ny + ty - 1) / ty) * ((p->nz + tz - 1) / tz);
+  b += 5 * 4 * (ntiles + 1) + 2 * 4 * vcap;
+  b += std::max<long long>(4 * 8 * N, 3 * 8 * vcap);
+  return b;
 }
 
 int hc_get_stats(hc_handle* h, hc_stats* out) {

@@ -150,6 +150,23 @@ __device__ __forceinline__ void pull(const LbmView<T>& L, const T* __restrict__ 
   }
 }
 
+// Mask bits of the 18 bounce-back links.
+constexpr uint32_t NB_LINKS = (1u << 18) - 1u;
+
+// True when node (X,Y,Z) with mask m can pull through the 32-bit offsets:
+// no bounce-back link and no neighbour across a face of the lattice.
+template <typename T>
+__device__ __forceinline__ bool pull_is_interior(const LbmView<T>& L, int X, int Y, int Z, uint32_t m) {
+  return (m & NB_LINKS) == 0u && X > 0 && X < L.nx - 1 && Y > 0 && Y < L.ny - 1 && Z > 0 && Z < L.nz - 1;
+}
+
+// pull() for an interior node when 19 N < 2^31: one 32-bit add per population.
+template <typename T>
+__device__ __forceinline__ void pull_interior(const LbmView<T>& L, const T* __restrict__ src, int n, T f[19]) {
+#pragma unroll
+  for (int j = 0; j < 19; ++j) f[j] = __ldg(src + (n + L.off[j]));
+}
+
 // rhoBar = sum f, j = sum c f over the shifted populations, pair-wise
 template <typename T>
 __device__ __forceinline__ void moments(const T f[19], T& rhoBar, T& jx, T& jy, T& jz) {

@@ -38,6 +38,10 @@ struct LbmView {
   int reverse;                   // sweep the lattice from the last z-plane down
   T omega;
   T uw[MAX_WALL_CLASSES][3];
+  // 32-bit pull offsets, valid when 19 N < 2^31 (fast != 0): population j of
+  // an interior node n (no wrap, no bounce-back link) is fsrc[n + off[j]]
+  int fast;
+  int off[19];
 };
 
 // Per-cell-type rest state and lattice-unit constants (device pointers).
@@ -167,5 +171,14 @@ cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* 
 
 // message returned by hc_last_error(NULL) for calls that take no handle
 void set_handleless_error(const std::string& msg);
+
+}  // namespace hcd
+
+struct hc_handle;
+namespace hcd {
+// what the serving batch needs to know of a handle
+cudaStream_t handle_stream(const hc_handle* h);
+int handle_device(const hc_handle* h);
+long long handle_bytes(const hc_handle* h);
 
 }  // namespace hcd

@@ -6,6 +6,7 @@
 //   moments / stream_out / stream_in / field conversions for readback and set-up
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "hc_d3q19.cuh"
 
@@ -21,15 +22,18 @@ namespace hcd {
 // (pull_rows); otherwise each thread pulls directly from global memory.
 // The sweep direction alternates every step (L.reverse): a pass then starts
 // on the planes the previous pass wrote last, which are still in L2.
-template <typename T, bool ROWS>
+template <typename T, bool ROWS, bool I32>
 __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
+  // I32: every population index fits 32 bits (19 N < 2^31), so interior
+  // nodes pull through L.off and all index arithmetic stays 32-bit
+  using Idx = typename std::conditional<I32, int, long long>::type;
   extern __shared__ double k1_smem[];
   const int X = blockIdx.x * blockDim.x + threadIdx.x;
   const int Y = blockIdx.y * blockDim.y + threadIdx.y;
   const int Z = L.reverse ? L.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
-  const long long N = L.N;
+  const Idx N = (Idx)L.N;
   T f[19];
-  long long n;
+  Idx n;
   uint32_t m;
   if (ROWS) {
     const bool inside = Y < L.ny;
@@ -42,10 +46,11 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
     if (!need) return;
   } else {
     if (X >= L.nx || Y >= L.ny) return;
-    n = (long long)X + (long long)L.nx * ((long long)Y + (long long)L.ny * Z);
+    n = (Idx)X + (Idx)L.nx * ((Idx)Y + (Idx)L.ny * Z);
     m = __ldg(L.nbmask + n);
     if (m & NB_SOLID) return;
-    pull(L, L.fsrc, X, Y, Z, n, m, f);
+    if (I32 && pull_is_interior(L, X, Y, Z, m)) pull_interior(L, L.fsrc, (int)n, f);
+    else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   }
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
@@ -99,13 +104,14 @@ cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStrea
     while (L.nx * by > 256 && by > 1) by /= 2;
     dim3 block(L.nx, by, 1);
     dim3 grid(1, (L.ny + by - 1) / by, L.nz);
-    k_collide_stream<T, true><<<grid, block, pull_rows_smem<T>(L.nx, by), s>>>(L);
+    k_collide_stream<T, true, false><<<grid, block, pull_rows_smem<T>(L.nx, by), s>>>(L);
     return cudaGetLastError();
   }
   if (bx <= 0) bx = 64;
   dim3 block(bx, by, 1);
   dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
-  k_collide_stream<T, false><<<grid, block, 0, s>>>(L);
+  if (L.fast) k_collide_stream<T, false, true><<<grid, block, 0, s>>>(L);
+  else k_collide_stream<T, false, false><<<grid, block, 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -114,17 +120,19 @@ cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStrea
 // tagged by this step's stencils (Palabos computeVelocity for Guo forcing,
 // core/hemoCellParticleField.cpp:833); L.fsrc is the post-collision state,
 // L.Fcur the force of that collision.
-template <typename T>
+template <typename T, bool I32>
 __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
-  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= L.N) return;
-  const long long n = L.reverse ? L.N - 1 - g : g;
+  using Idx = typename std::conditional<I32, int, long long>::type;
+  const Idx g = (Idx)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (Idx)L.N) return;
+  const Idx n = L.reverse ? (Idx)L.N - 1 - g : g;
   if (L.ntag[n] != *L.stamp) return;
   const uint32_t m = L.nbmask[n];
   int X, Y, Z;
-  node_xyz(n, L.nx, L.ny, X, Y, Z);
+  node_xyz((long long)n, L.nx, L.ny, X, Y, Z);
   T f[19];
-  pull(L, L.fsrc, X, Y, Z, n, m, f);
+  if (I32 && pull_is_interior(L, X, Y, Z, m)) pull_interior(L, L.fsrc, (int)n, f);
+  else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T rhoBar, jx, jy, jz, Fx, Fy, Fz;
   moments(f, rhoBar, jx, jy, jz);
   FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
@@ -134,7 +142,8 @@ __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
 }
 template <typename T>
 cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s) {
-  k_node_velocity<T><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
+  if (L.fast) k_node_velocity<T, true><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
+  else k_node_velocity<T, false><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
   return cudaGetLastError();
 }
 

@@ -173,6 +173,8 @@ class HemoCell:
 
     # --- lifecycle
     def close(self):
+        if getattr(self, "_batch", None) is not None:
+            return  # a Batch owns the handle until it is released
         if getattr(self, "_h", None):
             self._lib.hc_destroy(self._h)
             self._h = None
@@ -272,8 +274,11 @@ class HemoCell:
         self._check(self._lib.hc_profile_stages(self._h, nsteps, _dp(out)))
         return dict(zip(("spread", "collide_stream", "interp_advance", "mechanics", "step"), out.tolist()))
 
-    def read_positions(self, out: np.ndarray):
-        """Positions only, into a caller-owned (V,3) float64 buffer (pinned for speed)."""
+    def read_positions(self, out: Optional[np.ndarray] = None):
+        """Positions only, into a caller-owned (V,3) float64 buffer (pinned for
+        speed), or a new array when none is given."""
+        if out is None:
+            out = np.zeros((self.stats().vertices, 3))
         self._check(self._lib.hc_read_vertices(self._h, _dp(out), None, None))
         return out
 
@@ -358,3 +363,93 @@ class HemoCell:
     def set_tuning(self, t):
         t = np.ascontiguousarray(t, np.int32)
         self._check(self._lib.hc_set_tuning(self._h, _ip(t)))
+
+
+def estimate_device_bytes(dims, form: int, nvertices: int, ncells: int, tile=(8, 8, 8)) -> int:
+    """Upper bound of the device bytes of a handle (hc_estimate_device_bytes)."""
+    p = L.hc_params()
+    p.nx, p.ny, p.nz = dims
+    for a in range(3):
+        p.tile[a] = int(tile[a])
+    p.form = form
+    b = L.lib().hc_estimate_device_bytes(C.byref(p), int(nvertices), int(ncells))
+    if b < 0:
+        raise HemoCellError("invalid parameters for the estimate")
+    return int(b)
+
+
+class Batch:
+    """Continuous batching of independent solves on one device (hc_batch_*).
+
+    ``admit`` hands a set-up :class:`HemoCell` to the batch, which then owns
+    its handle; ``pump`` keeps every resident solve's stream fed and reports
+    how many finished; ``pop`` returns a finished solve (readable through its
+    ``read_*`` methods) and ``release`` frees it and its share of the budget.
+    """
+
+    def __init__(self, budget_bytes: int, max_slots: int = 64, chunk_steps: int = 50, device: int = 0):
+        self._lib = L.lib()
+        b = self._lib.hc_batch_create(device, int(budget_bytes), int(max_slots), int(chunk_steps))
+        if not b:
+            raise HemoCellError(self._lib.hc_last_error(None).decode())
+        self._b = C.c_void_p(b)
+        self._owned: dict[int, HemoCell] = {}
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            raise HemoCellError(self._lib.hc_batch_last_error(self._b).decode() or f"error {rc}")
+        return rc
+
+    def fits(self, nbytes: int) -> bool:
+        return self._check(self._lib.hc_batch_fits(self._b, int(nbytes))) == 1
+
+    def admit(self, hc: HemoCell, nsteps: int, tag: int) -> bool:
+        """True if admitted (the batch now owns hc's handle); False if it does
+        not fit the budget or the slots now (hc stays the caller's)."""
+        rc = self._lib.hc_batch_admit(self._b, hc._h, int(nsteps), int(tag))
+        if rc == L.HC_ERR_MEMORY:
+            return False
+        self._check(rc)
+        hc._batch = self
+        self._owned[hc._h.value] = hc
+        return True
+
+    def pump(self, wait_ms: float = 1.0) -> int:
+        return self._check(self._lib.hc_batch_pump(self._b, float(wait_ms)))
+
+    def pop(self):
+        """(tag, HemoCell, status) of one finished solve, or None."""
+        tag = C.c_longlong()
+        h = C.c_void_p()
+        st = C.c_int()
+        if self._check(self._lib.hc_batch_pop(self._b, C.byref(tag), C.byref(h), C.byref(st))) == 0:
+            return None
+        return tag.value, self._owned[h.value], st.value
+
+    def release(self, hc: HemoCell, destroy: bool = True):
+        key = hc._h.value
+        self._check(self._lib.hc_batch_release(self._b, hc._h, 1 if destroy else 0))
+        self._owned.pop(key, None)
+        hc._batch = None
+        if destroy:
+            hc._h = None
+
+    def stats(self) -> dict:
+        st = L.hc_batch_stats()
+        self._check(self._lib.hc_batch_get_stats(self._b, C.byref(st)))
+        return {n: getattr(st, n) for n, _ in L.hc_batch_stats._fields_}
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self._lib.hc_batch_destroy(self._b)
+            for hc in self._owned.values():
+                hc._batch = None
+                hc._h = None
+            self._owned.clear()
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

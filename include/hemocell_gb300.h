@@ -219,6 +219,46 @@ int hc_pack_cells(int nx, int ny, int nz, const int* periodic, const uint8_t* so
                   const int* type_nf, const int* counts, double margin, unsigned long long seed,
                   int max_attempts, double* centres, double* angles, int* types);
 
+/* --- serving: continuous batching of independent solves on one device.
+ * No counterpart in the reference (one simulation per MPI job).  A batch owns
+ * the handles admitted to it and steps them together: each solve keeps its own
+ * lattice, meshes and stream, and hc_batch_pump keeps every stream fed with
+ * chunks of `chunk_steps` steps (hc_step, graph replays in the batched launch
+ * mode), so the work of all resident solves overlaps on the device.  A batch is
+ * thread-compatible like a handle. */
+typedef struct hc_batch hc_batch;
+typedef struct hc_batch_stats {
+  int active, finished, popped, max_slots;
+  long long budget_bytes, bytes_in_use;
+  long long admitted, completed, refused, steps_enqueued;
+} hc_batch_stats;
+
+/* upper bound of the device bytes a handle with these parameters, vertices
+ * and cells holds, including the staging of hc_read_fluid, hc_read_vertices
+ * and hc_read_bins (not hc_read_populations); no device call */
+long long hc_estimate_device_bytes(const hc_params* p, int nvertices, int ncells);
+/* budget_bytes: device bytes the resident solves may hold (their handles'
+ * hc_stats.device_bytes); max_slots: resident solves at most */
+hc_batch* hc_batch_create(int device, long long budget_bytes, int max_slots, int chunk_steps);
+int hc_batch_destroy(hc_batch* b);              /* destroys every handle it still holds */
+const char* hc_batch_last_error(const hc_batch* b);
+/* 1 if a solve of `bytes` would be admitted now, else 0 */
+int hc_batch_fits(const hc_batch* b, long long bytes);
+/* admit a set-up handle for nsteps more steps; on HC_OK the batch owns it,
+ * on HC_ERR_MEMORY (over budget or no slot) the caller keeps it */
+int hc_batch_admit(hc_batch* b, hc_handle* h, int nsteps, long long tag);
+/* enqueue work and collect finished solves; waits up to wait_ms for at least
+ * one to finish.  Returns how many finished in this call (>= 0). */
+int hc_batch_pump(hc_batch* b, double wait_ms);
+/* take one finished solve: returns 1 and its tag, handle and status (HC_OK or
+ * the failure of its steps), or 0 if none is waiting.  Its steps are complete
+ * on the device; read it through the hc_read_* calls. */
+int hc_batch_pop(hc_batch* b, long long* tag, hc_handle** h, int* status);
+/* end the batch's hold of a popped solve and free its budget; destroy = 1
+ * destroys the handle, 0 hands it back to the caller */
+int hc_batch_release(hc_batch* b, hc_handle* h, int destroy);
+int hc_batch_get_stats(const hc_batch* b, hc_batch_stats* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,26 +27,7 @@ def _orc():
 
 
 def mixed_box(seed=5, n=(20, 18, 16), wall=True):
-    """Small box with all three cell types and (optionally) moving walls."""
-    C = _cases()
-    nx, ny, nz = n
-    if wall:
-        flags, walls = C.shear_walls(n, 5000.0)
-        periodic = (1, 1, 0)
-    else:
-        flags, walls, periodic = None, {}, (1, 1, 1)
-    types = [C.rbc_type(320), C.plt_type(80, radius_m=1.0e-6, aspect=0.4), C.wbc_type(320)]
-    rng = np.random.default_rng(seed)
-    cells = []
-    centres = [((nx - 1) / 2, (ny - 1) / 2 - 3.5, (nz - 1) / 2), ((nx - 1) / 2 + 4, (ny - 1) / 2 + 5, (nz - 1) / 2),
-               ((nx - 1) / 2 - 4.5, (ny - 1) / 2 + 4.0, (nz - 1) / 2 + 1)]
-    for t, c in enumerate(centres):
-        ang = rng.uniform(-np.pi, np.pi, size=(1, 3))
-        xyz = C.place_cells(types[t].mesh, np.array([c]), ang)
-        cells.append((t, xyz))
-    case = C.Case("mixed_box", n, periodic, flags=flags, walls=walls, types=types, cells=cells,
-                  body_mode=1, body=(2e-6, -1e-6, 5e-7))
-    return case
+    return _cases().mixed_box(seed=seed, n=n, wall=wall)
 
 
 def randomize(case, hc, o, seed=11, amp=2e-3, famp=1e-4, xamp=0.05, vamp=1e-3):
