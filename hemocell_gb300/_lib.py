@@ -35,6 +35,7 @@ HC_STAGE_ADVANCE = 3
 HC_STAGE_MECHANICS = 4
 HC_STAGE_MECHANICS_FORCED = 5
 HC_STAGE_BIN = 6
+HC_STAGE_REPULSION = 7
 
 
 class hc_params(C.Structure):
@@ -82,6 +83,9 @@ SIGNATURES = {
     "hc_add_cells_xyz": (C.c_int, [P, C.c_int, C.c_int, D]),
     "hc_set_timescales": (C.c_int, [P, I, C.c_int, C.c_int]),
     "hc_set_vertex_forces": (C.c_int, [P, C.c_int, I, D]),
+    "hc_set_repulsion": (C.c_int, [P, C.c_double, C.c_double, C.c_int]),
+    "hc_set_boundary_repulsion": (C.c_int, [P, C.c_double, C.c_double, C.c_int]),
+    "hc_read_repulsion": (C.c_int, [P, D]),
     "hc_step": (C.c_int, [P, C.c_int]),
     "hc_stage": (C.c_int, [P, C.c_int]),
     "hc_sync": (C.c_int, [P]),

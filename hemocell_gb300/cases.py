@@ -225,6 +225,18 @@ def mixed_box(seed: int = 5, n: Tuple[int, int, int] = (20, 18, 16), wall: bool 
                 body_mode=1, body=(2e-6, -1e-6, 5e-7))
 
 
+def repulsion_box() -> Case:
+    """Two RBCs (162 vertices) stacked close together in a 24x24x16 Couette box,
+    the lower one about a lattice unit from the bottom wall: the repulsion
+    parity case (inter-cell pairs and wall pushes both occur)."""
+    n = (24, 24, 16)
+    flags, walls = shear_walls(n, 2000.0)
+    t = rbc_type(320)
+    cells = [(0, place_cells(t.mesh, np.array([[11.5, 11.5, 3.6]]), np.zeros((1, 3)))),
+             (0, place_cells(t.mesh, np.array([[12.0, 11.0, 8.2]]), np.array([[0.1, -0.05, 0.2]])))]
+    return Case("repulsion_box", n, (1, 1, 0), flags=flags, walls=walls, types=[t], cells=cells)
+
+
 def stretch_cell(min_triangles: int = 600) -> Case:
     """Single RBC in a closed 52x26x26 box (tests/validation/stretch_cell):
     nuP 1.1e-6, dt 1e-7 -> tau 1.82; box faces are static walls; the cell is

@@ -310,6 +310,22 @@ class HemoCell {
     cellfields->particleVelocityUpdateTimescale = separation;
     if (h_ && cellfields->size()) pushTimescales();
   }
+  // core/hemoCell.cpp:420-426: cutoff in micrometres; the constant is used as
+  // given (lattice force units), every step unless a timescale is set
+  void setRepulsion(double repulsionConstant, double repulsionCutoff) {
+    repulsionConstant_ = repulsionConstant;
+    repulsionCutoff_ = repulsionCutoff * (1e-6 / Parameters::dx);
+    check(hc_set_repulsion(h_, repulsionConstant_, repulsionCutoff_, repulsionTimescale_));
+  }
+  void setRepulsionTimeScaleSeperation(unsigned int separation) {
+    repulsionTimescale_ = (int)separation;
+    if (repulsionCutoff_ > 0) check(hc_set_repulsion(h_, repulsionConstant_, repulsionCutoff_, repulsionTimescale_));
+  }
+  // core/hemoCell.cpp:428-436
+  void enableBoundaryParticles(double constant, double cutoff, unsigned int timestep = 1) {
+    check(hc_set_boundary_repulsion(h_, constant, cutoff * (1e-6 / Parameters::dx), (int)timestep));
+  }
+
   // setExternalVector(lattice, box, force) of the driver: a uniform body force
   void setExternalVector(double fx, double fy, double fz) {
     const double p[3] = {fx, fy, fz};
@@ -344,6 +360,8 @@ class HemoCell {
 
  private:
   hc_handle* h_ = nullptr;
+  double repulsionConstant_ = 0, repulsionCutoff_ = 0;
+  int repulsionTimescale_ = 1;
   int check(int rc) {
     if (rc < 0) die(std::string("(HemoCell) ") + hc_last_error(h_));
     return rc;

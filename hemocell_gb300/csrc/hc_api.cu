@@ -97,6 +97,21 @@ struct hc_handle {
   // k1 bx (0: row-staged, blocks of whole x-rows), k1 by, spread bs, ibm bs, mech bs, mech grid,
   // mech variant (0 vertex gather, 1 face/edge scatter)
   int tune[8] = {64, 2, 128, 128, 384, 0, 0, 0};
+  // repulsion (setRepulsion / enableBoundaryParticles): constants, cutoffs in
+  // lattice units, timescales (0 = off) and device state
+  double rep_k = 0, rep_rc = 0, brep_k = 0, brep_rc = 0;
+  int rep_every = 0, brep_every = 0;
+  int* rep_cnt = nullptr;
+  int* rep_slot = nullptr;
+  int* rep_vq = nullptr;
+  void* rep_xr = nullptr;
+  uint8_t* rep_bnode = nullptr;
+  void* frep_cell = nullptr;
+  void* frep_wall = nullptr;
+  long long rep_vcap = 0;
+  // bulk-copy collide-stream plan for tune[7] (stages | CTAs per SM << 4)
+  hcd::BulkPlan bulk{};
+  int bulk_key = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool graph_valid = false;
   long long device_bytes = 0;
@@ -216,6 +231,7 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   L.omega = (T)(1.0 / h->u.tau);
   for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
+  L.status = h->status;
   L.fast = 19LL * h->N < (1LL << 31) ? 1 : 0;
   const long long nxy = (long long)h->nx * h->ny;
   for (int j = 0; j < 19; ++j)
@@ -236,6 +252,8 @@ VertexView<T> vertex_view(hc_handle* h) {
   vv.vnode = h->vnode;
   vv.vtile = h->vtile;
   vv.status = h->status;
+  vv.frep_cell = h->rep_every > 0 ? (const T*)h->frep_cell : nullptr;
+  vv.frep_wall = h->brep_every > 0 ? (const T*)h->frep_wall : nullptr;
   return vv;
 }
 
@@ -375,6 +393,28 @@ int grow1(hc_handle* h, void** p, size_t es, long long oldn, long long newn, lon
   return HC_OK;
 }
 
+// Device state of the repulsion terms that are enabled, sized for the
+// vertex capacity (the kept forces are carried over when it grows).
+int ensure_repulsion(hc_handle* h) {
+  int rc;
+  const bool any = h->rep_every > 0 || h->brep_every > 0;
+  if (!any) return HC_OK;
+  if (h->rep_every > 0 && !h->rep_cnt) {
+    HC_CUDA(h, dalloc(h, (void**)&h->rep_cnt, sizeof(int) * h->N));
+    HC_CUDA(h, dalloc(h, (void**)&h->rep_slot, sizeof(int) * hcd::REP_SLOTS * h->N));
+  }
+  const long long cap = std::max<long long>(h->Vcap, 1);
+  if (h->rep_vcap < cap || !h->rep_vq) {
+    if ((rc = grow1(h, (void**)&h->rep_vq, 4, h->rep_vcap, cap, 0)) != HC_OK) return rc;
+    if ((rc = grow3(h, &h->rep_xr, h->ts, h->rep_vcap, cap, 0)) != HC_OK) return rc;
+    const int kept = (int)std::min<long long>(h->nvert, h->rep_vcap);
+    if ((rc = grow3(h, &h->frep_cell, h->ts, h->rep_vcap, cap, h->frep_cell ? kept : 0)) != HC_OK) return rc;
+    if ((rc = grow3(h, &h->frep_wall, h->ts, h->rep_vcap, cap, h->frep_wall ? kept : 0)) != HC_OK) return rc;
+    h->rep_vcap = cap;
+  }
+  return HC_OK;
+}
+
 int upload_types(hc_handle* h) {
   std::vector<TypeDev> tv(hcd::MAX_TYPES);
   for (size_t t = 0; t < h->types.size(); ++t) tv[t] = h->types[t].dev;
@@ -436,11 +476,33 @@ int enq_spread(hc_handle* h) {
 }
 
 template <typename T>
+cudaError_t launch_k1(hc_handle* h, const LbmView<T>& L) {
+  if (h->tune[7] != 0 && h->bulk_key == h->tune[7]) return hcd::launch_collide_stream_bulk<T>(L, h->bulk, h->stream);
+  return hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream);
+}
+
+template <typename T>
 int enq_collide(hc_handle* h) {
   LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
-  HC_CUDA(h, hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream));
+  HC_CUDA(h, launch_k1<T>(h, L));
   h->cur ^= 1;
   return HC_OK;
+}
+
+// Plan (and shared-memory attribute) of the bulk-copy collide-stream for
+// tune[7]; runs outside any stream capture.  Returns false when the lattice
+// does not allow that configuration.
+template <typename T>
+bool set_bulk_plan(hc_handle* h, int code) {
+  if (code == 0) return true;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
+  hcd::BulkPlan P;
+  if (!hcd::make_bulk_plan<T>(h->nx, h->ny, h->nz, code & 15, (code >> 4) * sms, &P)) return false;
+  if (hcd::prepare_collide_bulk<T>(P) != cudaSuccess) return false;
+  h->bulk = P;
+  h->bulk_key = code;
+  return true;
 }
 
 // post-stream view: populations f[cur], force of the last collision F[1-cur].
@@ -461,6 +523,31 @@ int enq_interp_advance(hc_handle* h, int do_interp, int do_advance, int mark = 0
 // The next spread can be fused into this mechanics pass when the batched
 // vertex-centric kernel handles every cell this step, every type is due
 // every step and no external vertex force is added before the spread.
+// The repulsion terms due at iteration `it` (core/hemoCell.cpp:307-312),
+// from the current positions; force = 1 recomputes every enabled term.
+template <typename T>
+int enq_repulsion(hc_handle* h, int it, bool force = false) {
+  const bool dc = h->rep_every > 0 && (force || it % h->rep_every == 0);
+  const bool dw = h->brep_every > 0 && (force || it % h->brep_every == 0);
+  if ((!dc && !dw) || h->nvert == 0) return HC_OK;
+  if (dc) HC_CUDA(h, cudaMemsetAsync(h->rep_cnt, 0, sizeof(int) * h->N, h->stream));
+  hcd::RepView<T> R;
+  R.cnt = dc ? h->rep_cnt : nullptr;
+  R.slot = h->rep_slot;
+  R.vq = h->rep_vq;
+  R.xr = (T*)h->rep_xr;
+  R.bnode = h->rep_bnode;
+  R.fcell = dc ? (T*)h->frep_cell : nullptr;
+  R.fwall = dw ? (T*)h->frep_wall : nullptr;
+  R.kc = (T)h->rep_k;
+  R.rc = (T)h->rep_rc;
+  R.kw = (T)h->brep_k;
+  R.rw = (T)h->brep_rc;
+  LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
+  HC_CUDA(h, hcd::launch_repulsion<T>(L, vertex_view<T>(h), R, h->stream));
+  return HC_OK;
+}
+
 bool fusable(hc_handle* h) {
   if (h->p.launch != HC_LAUNCH_BATCHED || h->tune[6] != 0 || h->next > 0 || h->ncells == 0) return false;
   if (h->velocity_every != 1) return false;
@@ -508,10 +595,16 @@ int enq_mechanics(hc_handle* h, bool forced, bool fuse = false) {
 template <typename T>
 int enq_step(hc_handle* h) {
   int rc;
-  if (!h->spread_done && (rc = enq_spread<T>(h)) != HC_OK) return rc;
+  if (!h->spread_done) {
+    if ((rc = enq_repulsion<T>(h, h->iter)) != HC_OK) return rc;
+    if ((rc = enq_spread<T>(h)) != HC_OK) return rc;
+  }
   if ((rc = enq_collide<T>(h)) != HC_OK) return rc;
   if ((rc = enq_interp_advance<T>(h, h->iter % h->velocity_every == 0, 1)) != HC_OK) return rc;
   const bool fuse = fusable(h);
+  // the fused spread is the next step's: its repulsion uses the positions
+  // just advanced, which are that step's positions
+  if (fuse && (rc = enq_repulsion<T>(h, h->iter + 1)) != HC_OK) return rc;
   if ((rc = enq_mechanics<T>(h, false, fuse)) != HC_OK) return rc;
   h->spread_done = fuse;
   h->iter++;
@@ -520,7 +613,7 @@ int enq_step(hc_handle* h) {
 
 bool graph_eligible(hc_handle* h) {
   if (h->p.launch != HC_LAUNCH_BATCHED) return false;
-  if (h->velocity_every != 1) return false;
+  if (h->velocity_every != 1 || h->rep_every > 1 || h->brep_every > 1) return false;
   for (TypeSlot& ts : h->types)
     if (ts.every != 1) return false;
   return true;
@@ -594,6 +687,8 @@ int run_stage(hc_handle* h, int stage) {
       return enq_mechanics<T>(h, false);
     case HC_STAGE_MECHANICS_FORCED:
       return enq_mechanics<T>(h, true);
+    case HC_STAGE_REPULSION:
+      return enq_repulsion<T>(h, h->iter, true);
     case HC_STAGE_BIN: {
       LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
       HC_CUDA(h, hcd::launch_bin_vertices<T>(L, vertex_view<T>(h), h->tg, h->stream));
@@ -679,6 +774,7 @@ int add_cells_positions(hc_handle* h, int type, int n, const std::vector<double>
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   h->nvert += n * nv;
   h->ncells += n;
+  if ((rc = ensure_repulsion(h)) != HC_OK) return rc;
   return upload_cell_lists(h);
 }
 
@@ -720,7 +816,7 @@ float time_it(hc_handle* h, int reps, int which) {
   auto once = [&]() {
     if (which == 0) {
       LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
-      hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream);
+      launch_k1<T>(h, L);
     } else if (which == 1) {
       LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
       hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream);
@@ -760,6 +856,7 @@ int autotune(hc_handle* h, const char* cache) {
     while (in >> k >> t[0] >> t[1] >> t[2] >> t[3] >> t[4] >> t[5] >> t[6] >> t[7])
       if (k == key) {
         std::memcpy(h->tune, t, sizeof(t));
+        if (!set_bulk_plan<T>(h, h->tune[7])) h->tune[7] = 0;
         invalidate_graph(h);
         return HC_OK;
       }
@@ -791,6 +888,23 @@ int autotune(hc_handle* h, const char* cache) {
   }
   h->tune[0] = bx;
   h->tune[1] = by;
+  // bulk-copy variant: stages x CTAs per SM
+  int b7 = 0;
+  h->tune[7] = 0;
+  for (int ctas : {1, 2})
+    for (int st : {3, 4, 6}) {
+      const int code = st | (ctas << 4);
+      if (!set_bulk_plan<T>(h, code)) continue;
+      h->tune[7] = code;
+      float t = time_it<T>(h, 5, 0);
+      if (t < best) {
+        best = t;
+        b7 = code;
+      }
+      h->tune[7] = 0;
+    }
+  h->tune[7] = b7;
+  if (b7 != 0) set_bulk_plan<T>(h, b7);
   if (h->nvert > 0) {
     best = 1e30f;
     int bb = h->tune[3];
@@ -1007,7 +1121,8 @@ int hc_destroy(hc_handle* h) {
                   h->fv,     h->vcell, h->vnode,     h->vtile,      h->cell_type,  h->cell_voff,
                   h->alive,  h->dcells_all, h->status, h->bin_counts, h->bin_cursor, h->bin_offsets,
                   h->tile_vertices, h->tile_cell_counts, h->tile_cell_offsets, h->tile_cells, h->scratch,
-                  h->ext_ids, h->ext_f};
+                  h->ext_ids, h->ext_f, h->rep_cnt, h->rep_slot, h->rep_vq, h->rep_xr, h->rep_bnode,
+                  h->frep_cell, h->frep_wall};
   for (void* q : ptrs) dfree(h, q);
   if (h->pool) release_pool(h->p.device, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1242,6 +1357,78 @@ int hc_set_vertex_forces(hc_handle* h, int n, const int* ids, const double* forc
   }
   h->next = n;
   invalidate_graph(h);
+  return HC_OK;
+}
+
+// HemoCell::setRepulsion (core/hemoCell.cpp:420-426); cutoff in lattice units
+int hc_set_repulsion(hc_handle* h, double k, double cutoff, int every) {
+  if (!h || !(cutoff >= 0)) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = undo_fused_spread(h)) != HC_OK) return rc;
+  h->rep_k = k;
+  h->rep_rc = cutoff;
+  h->rep_every = every > 0 ? every : 0;
+  invalidate_graph(h);
+  return ensure_repulsion(h);
+}
+
+// HemoCell::enableBoundaryParticles (core/hemoCell.cpp:428-436) with
+// populateBoundaryParticles (core/hemoCellParticleField.cpp:865-889): wall
+// nodes with a fluid node among their 26 neighbours (wrapped on periodic axes)
+int hc_set_boundary_repulsion(hc_handle* h, double k, double cutoff, int every) {
+  if (!h || !(cutoff >= 0)) return HC_ERR_INVALID;
+  int rc;
+  if ((rc = undo_fused_spread(h)) != HC_OK) return rc;
+  h->brep_k = k;
+  h->brep_rc = cutoff;
+  h->brep_every = every > 0 ? every : 0;
+  invalidate_graph(h);
+  if (h->brep_every == 0) return HC_OK;
+  std::vector<uint8_t> b(h->N, 0);
+  const int dims[3] = {h->nx, h->ny, h->nz};
+  for (int Z = 0; Z < h->nz; ++Z)
+    for (int Y = 0; Y < h->ny; ++Y)
+      for (int X = 0; X < h->nx; ++X) {
+        const long long n = X + (long long)h->nx * (Y + (long long)h->ny * Z);
+        if (h->hflag[n] == 0) continue;
+        bool near_fluid = false;
+        for (int dz = -1; dz <= 1 && !near_fluid; ++dz)
+          for (int dy = -1; dy <= 1 && !near_fluid; ++dy)
+            for (int dx = -1; dx <= 1 && !near_fluid; ++dx) {
+              int q[3] = {X + dx, Y + dy, Z + dz};
+              bool out = false;
+              for (int a = 0; a < 3; ++a)
+                if (q[a] < 0 || q[a] >= dims[a]) {
+                  if (h->p.periodic[a]) q[a] = (q[a] + dims[a]) % dims[a];
+                  else out = true;
+                }
+              if (!out && h->hflag[q[0] + (long long)h->nx * (q[1] + (long long)h->ny * q[2])] == 0) near_fluid = true;
+            }
+        b[n] = near_fluid ? 1 : 0;
+      }
+  if (!h->rep_bnode) HC_CUDA(h, dalloc(h, (void**)&h->rep_bnode, h->N));
+  HC_CUDA(h, cudaMemcpyAsync(h->rep_bnode, b.data(), h->N, cudaMemcpyHostToDevice, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  return ensure_repulsion(h);
+}
+
+// force_repulsion of every vertex, [V][3] (both terms summed)
+int hc_read_repulsion(hc_handle* h, double* f) {
+  if (!h || !f) return HC_ERR_INVALID;
+  const int V = h->nvert;
+  std::vector<double> sum((size_t)3 * V, 0.0);
+  int rc;
+  for (void* src : {h->rep_every > 0 ? h->frep_cell : nullptr, h->brep_every > 0 ? h->frep_wall : nullptr}) {
+    if (!src || V == 0) continue;
+    if ((rc = ensure_scratch(h, sizeof(double) * 3 * V)) != HC_OK) return rc;
+    if (h->f64) HC_CUDA(h, hcd::launch_soa_to_aos<double>((const double*)src, h->scratch, h->Vcap, V, h->stream));
+    else HC_CUDA(h, hcd::launch_soa_to_aos<float>((const float*)src, h->scratch, h->Vcap, V, h->stream));
+    std::vector<double> part((size_t)3 * V);
+    HC_CUDA(h, cudaMemcpyAsync(part.data(), h->scratch, 8 * part.size(), cudaMemcpyDeviceToHost, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (size_t k = 0; k < part.size(); ++k) sum[k] += part[k];
+  }
+  std::memcpy(f, sum.data(), 8 * sum.size());
   return HC_OK;
 }
 
@@ -1504,6 +1691,13 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
   if (in8[4] <= 0 || in8[4] > (h->f64 ? 384 : 768) || in8[4] % 32 != 0)
     return fail(h, HC_ERR_INVALID, "bad mechanics block size");
   if (in8[6] != 0 && in8[6] != 1) return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather) or 1 (scatter)");
+  if (in8[7] != 0) {
+    const int st = in8[7] & 15, ctas = in8[7] >> 4;
+    if (st < 2 || st > 8 || ctas < 1 || ctas > 4)
+      return fail(h, HC_ERR_INVALID, "bulk collide-stream code is stages (2-8) | CTAs per SM (1-4) << 4");
+    const bool ok = h->f64 ? set_bulk_plan<double>(h, in8[7]) : set_bulk_plan<float>(h, in8[7]);
+    if (!ok) return fail(h, HC_ERR_INVALID, "the lattice does not allow the bulk collide-stream (row bytes, rows, shared memory)");
+  }
   std::memcpy(h->tune, in8, sizeof(h->tune));
   invalidate_graph(h);
   return HC_OK;

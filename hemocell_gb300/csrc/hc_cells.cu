@@ -117,6 +117,17 @@ __global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const Vertex
     vv.f[V + i] = fy;
     vv.f[2 * V + i] = fz;
   }
+  // the repulsion force is spread with the clamped force (:857-859)
+  if (vv.frep_cell) {
+    fx += vv.frep_cell[i];
+    fy += vv.frep_cell[V + i];
+    fz += vv.frep_cell[2 * V + i];
+  }
+  if (vv.frep_wall) {
+    fx += vv.frep_wall[i];
+    fy += vv.frep_wall[V + i];
+    fz += vv.frep_wall[2 * V + i];
+  }
   Kern<T> K;
   ibm_weights(L, vv.x[i], vv.x[V + i], vv.x[2 * V + i], K);
   T* F = const_cast<T*>(L.Fcur);
@@ -133,6 +144,126 @@ cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f
   if (vv.nvert <= 0) return cudaSuccess;
   if (bs <= 0) bs = 128;
   k_spread<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, (T)f_limit);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Repulsion.  k_rep_bin bins every vertex of a live cell at its node
+// int(x + 0.5) (core/hemoCellParticleField.cpp:153-156), wrapped on periodic
+// axes, and keeps its position relative to that node.  k_repulsion then
+// gathers, per vertex, over the 27 nodes around its own: vertices of other
+// cells closer than the cutoff push with kc * (rc / d) along the separation,
+// counted twice when they share the node (the reference visits a node's own
+// pairs in both orders, :678-694), and boundary nodes closer than the wall
+// cutoff push with kw * (rw / d) (:891-918).  Node offsets of at most one in
+// each axis make the separation (x_p - q_p) - (x_b - q_b) - d exact in the
+// working precision and take the periodic image.  Each node's vertices are
+// visited in ascending index order so the sums are deterministic.
+template <typename T>
+__global__ void k_rep_bin(const LbmView<T> L, const VertexView<T> vv, const RepView<T> R) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= vv.nvert) return;
+  int q = -1;
+  if (vv.alive[vv.vcell[i]]) {
+    const long long V = vv.V;
+    const double P[3] = {vv.x[i], vv.x[V + i], vv.x[2 * V + i]};
+    const int n[3] = {L.nx, L.ny, L.nz};
+    int c[3];
+    T r[3];
+    bool in = true;
+    for (int a = 0; a < 3; ++a) {
+      const double b = floor(P[a] + 0.5);
+      r[a] = (T)(P[a] - b);
+      long long v = (long long)b;
+      if (L.per[a]) v = ((v % n[a]) + n[a]) % n[a];
+      else if (v < 0 || v >= n[a]) in = false;
+      c[a] = (int)v;
+    }
+    if (in) {
+      q = c[0] + L.nx * (c[1] + L.ny * c[2]);
+      for (int a = 0; a < 3; ++a) R.xr[a * V + i] = r[a];
+      if (R.cnt) {
+        const int s = atomicAdd(R.cnt + q, 1);
+        if (s < REP_SLOTS) R.slot[(long long)q * REP_SLOTS + s] = i;
+        else atomicOr(L.status, STATUS_REP_OVERFLOW);
+      }
+    }
+  }
+  R.vq[i] = q;
+}
+
+template <typename T>
+__global__ void k_repulsion(const LbmView<T> L, const VertexView<T> vv, const RepView<T> R) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= vv.nvert) return;
+  const long long V = vv.V;
+  const int q0 = R.vq[p];
+  T fc[3] = {T(0), T(0), T(0)}, fw[3] = {T(0), T(0), T(0)};
+  if (q0 >= 0) {
+    const int X0 = q0 % L.nx, Y0 = (q0 / L.nx) % L.ny, Z0 = q0 / (L.nx * L.ny);
+    const T rp[3] = {R.xr[p], R.xr[V + p], R.xr[2 * V + p]};
+    const int cp = vv.vcell[p];
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int d[3] = {dx, dy, dz};
+          const int c0[3] = {X0, Y0, Z0}, n[3] = {L.nx, L.ny, L.nz};
+          int c[3];
+          bool out = false;
+          for (int a = 0; a < 3; ++a) {
+            c[a] = c0[a] + d[a];
+            if (c[a] < 0 || c[a] >= n[a]) {
+              if (L.per[a]) c[a] = c[a] < 0 ? c[a] + n[a] : c[a] - n[a];
+              else out = true;
+            }
+          }
+          if (out) continue;
+          const int qb = c[0] + L.nx * (c[1] + L.ny * c[2]);
+          if (R.fcell) {
+            const int cnt = min(R.cnt[qb], REP_SLOTS);
+            const int* sl = R.slot + (long long)qb * REP_SLOTS;
+            const T mult = (dx == 0 && dy == 0 && dz == 0) ? T(2) : T(1);
+            int last = -1;
+            for (int k = 0; k < cnt; ++k) {
+              int b = 0x7fffffff;
+              for (int m = 0; m < cnt; ++m) {
+                const int v = sl[m];
+                if (v > last && v < b) b = v;
+              }
+              last = b;
+              if (vv.vcell[b] == cp) continue;
+              T dv[3];
+              for (int a = 0; a < 3; ++a) dv[a] = (rp[a] - R.xr[a * V + b]) - T(d[a]);
+              const T dist = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+              if (dist < R.rc) {
+                const T s = mult * R.kc * (R.rc / dist) / dist;
+                for (int a = 0; a < 3; ++a) fc[a] += dv[a] * s;
+              }
+            }
+          }
+          if (R.fwall && R.bnode[qb]) {
+            T dv[3];
+            for (int a = 0; a < 3; ++a) dv[a] = rp[a] - T(d[a]);
+            const T dist = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+            if (dist < R.rw) {
+              const T s = R.kw * (R.rw / dist) / dist;
+              for (int a = 0; a < 3; ++a) fw[a] += dv[a] * s;
+            }
+          }
+        }
+  }
+  for (int a = 0; a < 3; ++a) {
+    if (R.fcell) R.fcell[a * V + p] = fc[a];
+    if (R.fwall) R.fwall[a * V + p] = fw[a];
+  }
+}
+
+template <typename T>
+cudaError_t launch_repulsion(const LbmView<T>& L, const VertexView<T>& vv, const RepView<T>& R, cudaStream_t s) {
+  if (vv.nvert <= 0) return cudaSuccess;
+  const int g = (vv.nvert + 255) / 256;
+  k_rep_bin<T><<<g, 256, 0, s>>>(L, vv, R);
+  k_repulsion<T><<<g, 256, 0, s>>>(L, vv, R);
   return cudaGetLastError();
 }
 
@@ -642,6 +773,9 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
         mag += f.z * f.z;
         mag = sqrt(mag);
         if (mag > M.f_limit) f = vscale(f, M.f_limit / mag);
+        const int gi = voff + i;
+        if (vv.frep_cell) f = f + V3t<T>{vv.frep_cell[gi], vv.frep_cell[V + gi], vv.frep_cell[2 * V + gi]};
+        if (vv.frep_wall) f = f + V3t<T>{vv.frep_wall[gi], vv.frep_wall[V + gi], vv.frep_wall[2 * V + gi]};
         Kern<T> K;
         ibm_weights(M.L, vv.x[voff + i], vv.x[V + voff + i], vv.x[2 * V + voff + i], K);
         const uint32_t stamp = *M.L.stamp;
@@ -1102,6 +1236,8 @@ cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* 
 #define HC_CELL_INST(T)                                                                                        \
   template cudaError_t launch_spread<T>(const LbmView<T>&, const VertexView<T>&, double, int, cudaStream_t);   \
   template cudaError_t launch_mark_nodes<T>(const LbmView<T>&, const VertexView<T>&, cudaStream_t);            \
+  template cudaError_t launch_repulsion<T>(const LbmView<T>&, const VertexView<T>&, const RepView<T>&,          \
+                                           cudaStream_t);                                                      \
   template cudaError_t launch_add_vertex_forces<T>(const VertexView<T>&, const int*, const double*, int,       \
                                                    cudaStream_t);                                              \
   template cudaError_t launch_interp_advance<T>(const LbmView<T>&, const VertexView<T>&, const TileGrid&, int, \

@@ -42,6 +42,22 @@ struct LbmView {
   // an interior node n (no wrap, no bounce-back link) is fsrc[n + off[j]]
   int fast;
   int off[19];
+  unsigned int* status;  // device status word (bit 2: a pipeline wait timed out)
+};
+
+// status bits shared by the kernels and hc_device_status
+constexpr unsigned int STATUS_NONFINITE = 1u;
+constexpr unsigned int STATUS_CELL_DELETED = 2u;
+constexpr unsigned int STATUS_WAIT_TIMEOUT = 4u;
+
+// Launch plan of the bulk-copy collide-stream kernel (k_collide_stream_bulk):
+// each CTA owns a slab of R whole x-rows and sweeps a chunk of zlen planes,
+// staging the 19 source rows of every plane in shared memory, `stages` planes ahead.
+struct BulkPlan {
+  int R, nslab, zlen, zchunks, stages;
+  int stage_bytes;  // bytes of one stage in shared memory
+  int tx_bytes;     // bytes the copies of one stage deliver
+  long long spin_limit;
 };
 
 // Per-cell-type rest state and lattice-unit constants (device pointers).
@@ -90,6 +106,28 @@ struct VertexView {
   int* vnode;         // per vertex nearest node (or -1)
   int* vtile;         // per vertex tile (or -1)
   unsigned int* status;
+  const T* frep_cell;  // [3][V] repulsion added to the spread force (may be null)
+  const T* frep_wall;  // [3][V]
+};
+
+// Repulsion (applyRepulsionForce / applyBoundaryRepulsionForce,
+// core/hemoCellParticleField.cpp:677-743, 891-918): vertices binned per node
+// into REP_SLOTS slots (the reference's per-node hemo::Array<unsigned,10>,
+// core/hemoCellParticleField.cpp:140); a node holding more sets
+// STATUS_REP_OVERFLOW.
+constexpr int REP_SLOTS = 10;
+constexpr unsigned int STATUS_REP_OVERFLOW = 8u;
+
+template <typename T>
+struct RepView {
+  int* cnt;              // [N] vertices binned per node (null: no inter-cell term)
+  int* slot;             // [N][REP_SLOTS]
+  int* vq;               // [V] node of each vertex, -1 when not binned
+  T* xr;                 // [3][V] position relative to that node
+  const uint8_t* bnode;  // [N] 1 on boundary nodes (wall term)
+  T* fcell;              // [3][V] inter-cell term to recompute (null: keep)
+  T* fwall;              // [3][V] wall term to recompute (null: keep)
+  T kc, rc, kw, rw;      // constants and cutoffs (lattice units)
 };
 
 struct TileGrid {
@@ -118,6 +156,16 @@ struct MechView {
 // hc_lattice.cu
 template <typename T>
 cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStream_t s);
+// bulk-copy variant: false when the lattice does not allow it (nx * sizeof
+// row not a multiple of 16 bytes, no row count dividing ny, shared memory)
+template <typename T>
+bool make_bulk_plan(int nx, int ny, int nz, int stages, int ctas_target, BulkPlan* P);
+template <typename T>
+size_t bulk_smem_bytes(const BulkPlan& P);
+template <typename T>
+cudaError_t prepare_collide_bulk(const BulkPlan& P);
+template <typename T>
+cudaError_t launch_collide_stream_bulk(const LbmView<T>& L, const BulkPlan& P, cudaStream_t s);
 template <typename T>
 cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s);
 template <typename T>
@@ -157,6 +205,8 @@ template <typename T>
 cudaError_t launch_soa_to_aos(const T* src, double* dst, long long V, int n, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bin_vertices(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, cudaStream_t s);
+template <typename T>
+cudaError_t launch_repulsion(const LbmView<T>& L, const VertexView<T>& vv, const RepView<T>& R, cudaStream_t s);
 // binning: tile CSR sorted by (tile, cell, vertex)
 cudaError_t launch_bin_csr(const int* vtile, int nvert, int ntiles, int* counts, int* offsets, int* cursor,
                            int* tile_vertices, const int* vcell, int* tile_cell_counts, cudaStream_t s);

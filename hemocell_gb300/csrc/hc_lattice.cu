@@ -4,13 +4,61 @@
 //                      force field (body force), fusing the force reset.
 //   node_velocity      post-stream velocity of the nodes the IBM stencils touch
 //   moments / stream_out / stream_in / field conversions for readback and set-up
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <type_traits>
 
+#include "hc_async.cuh"
 #include "hc_d3q19.cuh"
 
 namespace hcd {
+
+// Guo-forced BGK collision of one node from its pulled populations f and
+// force F; writes the post-collision populations and the node's next force
+// (the body force of plane Z).
+template <typename T, typename Idx>
+__device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z, const T f[19], T Fx, T Fy, T Fz) {
+  const Idx N = (Idx)L.N;
+  T rhoBar, jx, jy, jz;
+  moments(f, rhoBar, jx, jy, jz);
+  const T rho = T(1) + rhoBar;
+  const T invRho = T(1) / rho;
+  const T ux = (jx + T(0.5) * Fx) * invRho;
+  const T uy = (jy + T(0.5) * Fy) * invRho;
+  const T uz = (jz + T(0.5) * Fz) * invRho;
+  const T uu = ux * ux + uy * uy + uz * uz;
+  const T uF = ux * Fx + uy * Fy + uz * Fz;
+  const T om = L.omega;
+  const T om1 = T(1) - om;
+  const T hs = T(1) - T(0.5) * om;
+  const T A = rhoBar - T(1.5) * rho * uu;  // even equilibrium part without w
+  const T B = T(4.5) * rho;
+  const T K = T(3) * rho * om;
+  const T G = T(-3) * hs * uF;
+  const T H = T(9) * hs;
+  const T Lc = T(3) * hs;
+  const T w1 = T(1.0 / 18.0);
+  const T Aw1 = om * w1 * A, Bw1 = om * w1 * B, Gw1 = w1 * G, Hw1 = w1 * H, Kw1 = w1 * K, Lw1 = w1 * Lc;
+  const T Aw2 = T(0.5) * Aw1, Bw2 = T(0.5) * Bw1, Gw2 = T(0.5) * Gw1, Hw2 = T(0.5) * Hw1, Kw2 = T(0.5) * Kw1,
+          Lw2 = T(0.5) * Lw1;
+
+  L.fdst[n] = om1 * f[0] + T(1.0 / 3.0) * (om * A + G);
+#pragma unroll
+  for (int i = 1; i <= 9; ++i) {
+    const int j = i + 9;  // c = c_j
+    const T cu = cdot(cxi(j), cyi(j), czi(j), ux, uy, uz);
+    const T cF = cdot(cxi(j), cyi(j), czi(j), Fx, Fy, Fz);
+    const bool axis = (wi(j) > 1.0 / 20.0);
+    const T Aw = axis ? Aw1 : Aw2, Bw = axis ? Bw1 : Bw2, Gw = axis ? Gw1 : Gw2;
+    const T Hw = axis ? Hw1 : Hw2, Kw = axis ? Kw1 : Kw2, Lw = axis ? Lw1 : Lw2;
+    const T P = (Bw * (cu * cu) + Aw) + (Hw * (cu * cF) + Gw);
+    const T Q = Kw * cu + Lw * cF;
+    L.fdst[j * N + n] = om1 * f[j] + (P + Q);
+    L.fdst[i * N + n] = om1 * f[i] + (P - Q);
+  }
+  FieldLayout<T>::store(L.Fnext, N, n, L.bodyz[Z], L.bodyz[L.nz + Z], L.bodyz[2 * L.nz + Z]);
+}
 
 // ---------------------------------------------------------------------------
 // K1.  One thread per node; blocks (bx, by) over x,y and one z-plane per
@@ -54,45 +102,195 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
   }
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
+  collide_store<T, Idx>(L, n, Z, f, Fx, Fy, Fz);
+}
 
-  T rhoBar, jx, jy, jz;
-  moments(f, rhoBar, jx, jy, jz);
-  const T rho = T(1) + rhoBar;
-  const T invRho = T(1) / rho;
-  const T ux = (jx + T(0.5) * Fx) * invRho;
-  const T uy = (jy + T(0.5) * Fy) * invRho;
-  const T uz = (jz + T(0.5) * Fz) * invRho;
-  const T uu = ux * ux + uy * uy + uz * uz;
-  const T uF = ux * Fx + uy * Fy + uz * Fz;
-  const T om = L.omega;
-  const T om1 = T(1) - om;
-  const T hs = T(1) - T(0.5) * om;
-  const T A = rhoBar - T(1.5) * rho * uu;  // even equilibrium part without w
-  const T B = T(4.5) * rho;
-  const T K = T(3) * rho * om;
-  const T G = T(-3) * hs * uF;
-  const T H = T(9) * hs;
-  const T Lc = T(3) * hs;
-  const T w1 = T(1.0 / 18.0);
-  const T Aw1 = om * w1 * A, Bw1 = om * w1 * B, Gw1 = w1 * G, Hw1 = w1 * H, Kw1 = w1 * K, Lw1 = w1 * Lc;
-  const T Aw2 = T(0.5) * Aw1, Bw2 = T(0.5) * Bw1, Gw2 = T(0.5) * Gw1, Hw2 = T(0.5) * Hw1, Kw2 = T(0.5) * Kw1,
-          Lw2 = T(0.5) * Lw1;
+// ---------------------------------------------------------------------------
+// K1 with bulk copies.  A persistent CTA owns a slab of R whole x-rows
+// (y in [y0, y0+R)) and sweeps a chunk of z-planes.  For plane z, direction j
+// pulls from rows y - cy_j of plane z - cz_j of population array j: one
+// contiguous block of R rows (two when the slab touches the y edge and the
+// rows wrap), fetched whole by cp.async.bulk into a shared-memory stage
+// together with the plane's force and mask rows.  The x-shift -cx_j is then
+// read from the staged row, wrapping inside it.  One thread keeps `stages`
+// planes in flight; every thread computes one node of the slab from shared
+// memory and writes the post-collision populations as K1 does.  Bounce-back
+// links read the node's own opposite population from global memory.
+template <typename T>
+__device__ __forceinline__ T bounce_value(const LbmView<T>& L, int i, int X, int Y, int Z, long long n, uint32_t m) {
+  const Nbr nb(X, Y, Z, L.nx, L.ny, L.nz);
+  const uint32_t c = wall_class(L, i, X, Y, Z, nb, m >> NB_CLASS_SHIFT);
+  const T cuw = T(cxi(i)) * L.uw[c][0] + T(cyi(i)) * L.uw[c][1] + T(czi(i)) * L.uw[c][2];
+  return L.fsrc[i * L.N + n] - T(6.0 * wi(i)) * cuw;
+}
 
-  L.fdst[n] = om1 * f[0] + T(1.0 / 3.0) * (om * A + G);
-#pragma unroll
-  for (int i = 1; i <= 9; ++i) {
-    const int j = i + 9;  // c = c_j
-    const T cu = cdot(cxi(j), cyi(j), czi(j), ux, uy, uz);
-    const T cF = cdot(cxi(j), cyi(j), czi(j), Fx, Fy, Fz);
-    const bool axis = (wi(j) > 1.0 / 20.0);
-    const T Aw = axis ? Aw1 : Aw2, Bw = axis ? Bw1 : Bw2, Gw = axis ? Gw1 : Gw2;
-    const T Hw = axis ? Hw1 : Hw2, Kw = axis ? Kw1 : Kw2, Lw = axis ? Lw1 : Lw2;
-    const T P = (Bw * (cu * cu) + Aw) + (Hw * (cu * cF) + Gw);
-    const T Q = Kw * cu + Lw * cF;
-    L.fdst[j * N + n] = om1 * f[j] + (P + Q);
-    L.fdst[i * N + n] = om1 * f[i] + (P - Q);
+template <typename T>
+struct StageLayout {
+  int RN;
+  __device__ __host__ size_t pops() const { return 0; }
+  __device__ __host__ size_t force() const { return (size_t)19 * RN * sizeof(T); }
+  __device__ __host__ size_t mask() const { return force() + (size_t)RN * (sizeof(T) == 4 ? 16 : 24); }
+  __device__ __host__ size_t bytes() const { return mask() + (size_t)RN * 4; }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_collide_stream_bulk(const LbmView<T> L, const BulkPlan P) {
+  extern __shared__ __align__(128) unsigned char k1b_smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(k1b_smem);
+  unsigned char* stage0 = k1b_smem + 128;
+  const int nx = L.nx, ny = L.ny, nz = L.nz;
+  const int RN = P.R * nx;
+  const StageLayout<T> SL{RN};
+  const int tid = threadIdx.x;
+  const int slab = blockIdx.x % P.nslab;
+  const int zb = (blockIdx.x / P.nslab) * P.zlen;
+  const int y0 = slab * P.R;
+  const int zcount = min(P.zlen, nz - zb);
+  if (zcount <= 0) return;
+  const long long N = L.N;
+  if (tid == 0) {
+    for (int s = 0; s < P.stages; ++s) mbar_init(&bars[s], 1);
+    mbar_fence_init();
   }
-  FieldLayout<T>::store(L.Fnext, N, n, L.bodyz[Z], L.bodyz[L.nz + Z], L.bodyz[2 * L.nz + Z]);
+  __syncthreads();
+  auto plane_of = [&](int k) { return L.reverse ? zb + zcount - 1 - k : zb + k; };
+  // thread 0: fill the stage of plane k
+  auto issue = [&](int k) {
+    const int s = k % P.stages;
+    unsigned char* st = stage0 + (size_t)s * P.stage_bytes;
+    const int z = plane_of(k);
+    mbar_expect_tx(&bars[s], (uint32_t)P.tx_bytes);
+    const uint32_t rowb = (uint32_t)(nx * sizeof(T));
+#pragma unroll 1
+    for (int j = 0; j < 19; ++j) {
+      int zs = z - czi(j);
+      zs = zs < 0 ? zs + nz : (zs >= nz ? zs - nz : zs);
+      const int ys = y0 - cyi(j);
+      T* dst = reinterpret_cast<T*>(st + SL.pops()) + (size_t)j * RN;
+      const T* base = L.fsrc + (long long)j * N + (long long)zs * ny * nx;
+      if (ys >= 0 && ys + P.R <= ny) {
+        bulk_g2s(dst, base + (long long)ys * nx, (uint32_t)P.R * rowb, &bars[s]);
+      } else if (ys < 0) {  // the slab's first row comes from the last row
+        bulk_g2s(dst, base + (long long)(ny - 1) * nx, rowb, &bars[s]);
+        if (P.R > 1) bulk_g2s(dst + nx, base, (uint32_t)(P.R - 1) * rowb, &bars[s]);
+      } else {  // the slab's last row comes from the first row
+        if (P.R > 1) bulk_g2s(dst, base + (long long)ys * nx, (uint32_t)(P.R - 1) * rowb, &bars[s]);
+        bulk_g2s(dst + (size_t)(P.R - 1) * nx, base, rowb, &bars[s]);
+      }
+    }
+    const long long off = ((long long)z * ny + y0) * nx;
+    if (sizeof(T) == 4) {
+      bulk_g2s(st + SL.force(), reinterpret_cast<const float4*>(L.Fcur) + off, (uint32_t)RN * 16u, &bars[s]);
+    } else {
+      for (int a = 0; a < 3; ++a)
+        bulk_g2s(st + SL.force() + (size_t)a * RN * 8, L.Fcur + a * N + off, (uint32_t)RN * 8u, &bars[s]);
+    }
+    bulk_g2s(st + SL.mask(), L.nbmask + off, (uint32_t)RN * 4u, &bars[s]);
+  };
+  int issued = 0;
+  if (tid == 0)
+    for (; issued < min(P.stages, zcount); ++issued) issue(issued);
+  const int r = tid / nx, X = tid - r * nx, Y = y0 + r;
+  int k = 0;
+  bool failed = false;
+  for (; k < zcount; ++k) {
+    const int s = k % P.stages;
+    const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((k / P.stages) & 1), P.spin_limit);
+    const unsigned char* st = stage0 + (size_t)s * P.stage_bytes;
+    const uint32_t m = reinterpret_cast<const uint32_t*>(st + SL.mask())[tid];
+    const int Z = plane_of(k);
+    if (ok && !(m & NB_SOLID)) {
+      const T* sp = reinterpret_cast<const T*>(st + SL.pops());
+      const long long n = (long long)X + (long long)nx * ((long long)Y + (long long)ny * Z);
+      T f[19];
+      f[0] = sp[tid];
+#pragma unroll
+      for (int j = 1; j < 19; ++j) {
+        const int i = oppi(j);
+        if (m & (1u << (i - 1))) {
+          f[j] = bounce_value(L, i, X, Y, Z, n, m);
+        } else {
+          int xs = X - cxi(j);
+          xs = xs < 0 ? xs + nx : (xs >= nx ? xs - nx : xs);
+          f[j] = sp[j * RN + r * nx + xs];
+        }
+      }
+      T Fx, Fy, Fz;
+      if (sizeof(T) == 4) {
+        const float4 v = reinterpret_cast<const float4*>(st + SL.force())[tid];
+        Fx = (T)v.x;
+        Fy = (T)v.y;
+        Fz = (T)v.z;
+      } else {
+        const T* fp = reinterpret_cast<const T*>(st + SL.force());
+        Fx = fp[tid];
+        Fy = fp[RN + tid];
+        Fz = fp[2 * RN + tid];
+      }
+      collide_store<T, long long>(L, n, Z, f, Fx, Fy, Fz);
+    }
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    if (tid == 0 && issued < zcount) issue(issued++);
+  }
+  if (failed && tid == 0) {
+    atomicOr(L.status, STATUS_WAIT_TIMEOUT);
+    // let the copies already issued land before the CTA's shared memory is released
+    for (int q = k; q < issued; ++q)
+      if (!mbar_wait_bounded(&bars[q % P.stages], (uint32_t)((q / P.stages) & 1), P.spin_limit)) break;
+  }
+}
+
+template <typename T>
+bool make_bulk_plan(int nx, int ny, int nz, int stages, int ctas_target, BulkPlan* P) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || stages < 2 || ctas_target < 1) return false;
+  if ((nx * sizeof(T)) % 16 != 0 || nx > 256) return false;
+  int R = 0;
+  for (int r = 256 / nx; r >= 1; --r)
+    if (ny % r == 0) {
+      R = r;
+      break;
+    }
+  if (R == 0) return false;
+  const int RN = R * nx;
+  StageLayout<T> SL{RN};
+  P->R = R;
+  P->nslab = ny / R;
+  P->stages = stages;
+  P->stage_bytes = (int)((SL.bytes() + 127) / 128 * 128);
+  P->tx_bytes = (int)SL.bytes();
+  if (128 + (size_t)stages * P->stage_bytes > 227 * 1024) return false;
+  const int zch = std::max(1, std::min(nz, (ctas_target + P->nslab - 1) / P->nslab));
+  P->zlen = (nz + zch - 1) / zch;
+  P->zchunks = (nz + P->zlen - 1) / P->zlen;
+  P->spin_limit = 2000000000LL;
+  return true;
+}
+
+template <typename T>
+size_t bulk_smem_bytes(const BulkPlan& P) {
+  return 128 + (size_t)P.stages * P.stage_bytes;
+}
+
+// The attribute is device-wide state shared by every handle: raise it to the
+// opt-in maximum once rather than to one plan's size, which a later handle
+// with a smaller plan would lower beneath this one's.
+template <typename T>
+cudaError_t prepare_collide_bulk(const BulkPlan& P) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if ((int)bulk_smem_bytes<T>(P) > optin) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(k_collide_stream_bulk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+}
+
+template <typename T>
+cudaError_t launch_collide_stream_bulk(const LbmView<T>& L, const BulkPlan& P, cudaStream_t s) {
+  k_collide_stream_bulk<T><<<P.nslab * P.zchunks, P.R * L.nx, bulk_smem_bytes<T>(P), s>>>(L, P);
+  return cudaGetLastError();
 }
 
 // bx == 0 selects the row-staged kernel with blocks of (nx, by) when nx
@@ -314,6 +512,10 @@ cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream
 
 #define HC_LAT_INST(T)                                                                                    \
   template cudaError_t launch_collide_stream<T>(const LbmView<T>&, int, int, cudaStream_t);              \
+  template bool make_bulk_plan<T>(int, int, int, int, int, BulkPlan*);                                    \
+  template size_t bulk_smem_bytes<T>(const BulkPlan&);                                                     \
+  template cudaError_t prepare_collide_bulk<T>(const BulkPlan&);                                           \
+  template cudaError_t launch_collide_stream_bulk<T>(const LbmView<T>&, const BulkPlan&, cudaStream_t);   \
   template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                         \
   template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);             \
   template cudaError_t launch_stream_out<T>(const LbmView<T>&, double*, cudaStream_t);                   \

@@ -166,6 +166,7 @@ class HemoCell:
             raise HemoCellError(self._lib.hc_last_error(None).decode())
         self._h = C.c_void_p(h)
         self.nx, self.ny, self.nz = nx, ny, nz
+        self.dx = dx
         self.N = nx * ny * nz
         self.form = form
         self.types: list[Mesh] = []
@@ -254,6 +255,20 @@ class HemoCell:
                                                    _dp(forces) if len(ids) else None))
 
     # --- stepping
+    def setRepulsion(self, repulsionConstant: float, repulsionCutoff: float, timescale: int = 1):
+        """HemoCell::setRepulsion: cutoff in micrometres (converted with dx)."""
+        self._check(self._lib.hc_set_repulsion(self._h, repulsionConstant, repulsionCutoff * 1e-6 / self.dx,
+                                               int(timescale)))
+
+    def enableBoundaryParticles(self, constant: float, cutoff: float, timestep: int = 1):
+        """HemoCell::enableBoundaryParticles: cutoff in micrometres."""
+        self._check(self._lib.hc_set_boundary_repulsion(self._h, constant, cutoff * 1e-6 / self.dx, int(timestep)))
+
+    def read_repulsion(self) -> np.ndarray:
+        out = np.zeros((self.stats().vertices, 3))
+        self._check(self._lib.hc_read_repulsion(self._h, _dp(out)))
+        return out
+
     def iterate(self, nsteps: int = 1):
         self._check(self._lib.hc_step(self._h, nsteps))
 

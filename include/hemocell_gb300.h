@@ -54,6 +54,7 @@ extern "C" {
 #define HC_STAGE_MECHANICS 4      /* applyConstitutiveModel (due types) */
 #define HC_STAGE_MECHANICS_FORCED 5 /* applyConstitutiveModel(forced=true) */
 #define HC_STAGE_BIN 6            /* tile CSR + per-tile cell lists */
+#define HC_STAGE_REPULSION 7      /* applyRepulsionForce + applyBoundaryRepulsionForce */
 
 typedef struct hc_handle hc_handle;
 
@@ -128,6 +129,18 @@ int hc_set_timescales(hc_handle* h, const int* material_every, int ntypes, int v
  * (ids are global vertex indices, forces n*3 in lattice units); n = 0 clears */
 int hc_set_vertex_forces(hc_handle* h, int n, const int* ids, const double* forces);
 
+/* HemoCell::setRepulsion (core/hemoCell.cpp:420-426): vertices of different
+ * cells closer than `cutoff` (lattice units; the reference takes micrometres
+ * and multiplies by 1e-6/dx) repel with k * cutoff / d, recomputed every
+ * `every` steps (0 disables); applied with the spread like the reference's
+ * force_repulsion (core/hemoCellParticleField.cpp:677-743, :857-859) */
+int hc_set_repulsion(hc_handle* h, double k, double cutoff, int every);
+/* HemoCell::enableBoundaryParticles (core/hemoCell.cpp:428-436): the same
+ * push from wall nodes next to fluid (core/hemoCellParticleField.cpp:865-918) */
+int hc_set_boundary_repulsion(hc_handle* h, double k, double cutoff, int every);
+/* force_repulsion of every vertex, [V][3] */
+int hc_read_repulsion(hc_handle* h, double* f);
+
 /* --- the hot path: HemoCell::iterate() (core/hemoCell.cpp:299-376) */
 int hc_step(hc_handle* h, int nsteps);
 int hc_stage(hc_handle* h, int stage); /* one stage, for stage-wise parity */
@@ -183,12 +196,18 @@ int hc_bin_tiles_noalloc(const int* vertex_tile, const int* vertex_cell, int nve
                          int* tile_offsets, int* tile_vertices, int* tile_cell_offsets, int* tile_cells,
                          int max_tile_cells, void* stream);
 int hc_get_stats(hc_handle* h, hc_stats* out);
-/* last device status word: bit0 non-finite vertex velocity, bit1 cell deleted at a wall */
+/* device status word, sticky: bit0 non-finite vertex velocity, bit1 cell
+ * deleted at a wall, bit2 a shared-memory pipeline wait of the bulk-copy
+ * collide-stream timed out (the step's results are then invalid) */
 int hc_device_status(hc_handle* h, unsigned int* status);
 
 /* --- launch tuning (project autotuner; results cached on disk) */
 int hc_autotune(hc_handle* h, const char* cache_path);
 int hc_get_tuning(hc_handle* h, int* out8);
+/* in8: collide-stream block (bx, by; bx = 0 whole rows), spread block,
+ * interpolation block, mechanics block, mechanics grid (0 = one CTA per cell),
+ * mechanics variant (0 vertex gather, 1 face/edge scatter), bulk-copy
+ * collide-stream (0 off, else stages | CTAs per SM << 4) */
 int hc_set_tuning(hc_handle* h, const int* in8);
 
 /* --- mesh helpers (helper/meshGeneratingFunctions.hh:31-271).  Buffers are

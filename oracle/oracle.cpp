@@ -266,6 +266,12 @@ struct orc_sim {
   std::vector<std::pair<int, V3>> ext;  // external vertex forces
   // IBM kernel cache of the last spread (core/hemoCellParticle.h:75-76)
   std::vector<std::vector<std::pair<long, double>>> kern;
+  // repulsion (HemoCell::setRepulsion / enableBoundaryParticles,
+  // core/hemoCell.cpp:420-436): constant, cutoff (lattice units), timescale
+  double rep_const = 0, rep_cutoff = 0, brep_const = 0, brep_cutoff = 0;
+  int rep_every = 0, brep_every = 0;  // 0 = disabled
+  std::vector<V3> frep_cell, frep_wall;  // force_repulsion of each vertex, per source
+  std::vector<long> boundary_nodes;       // populateBoundaryParticles
 
   long idx(long X, long Y, long Z) const { return X + nx * (Y + (long)ny * Z); }
   void bodyAt(long Z, double* b) const {
@@ -423,12 +429,153 @@ void spread(orc_sim* s) {
     kernelWeights(s, s->x[i], s->kern[i]);
     const double mag = norm(s->fv[i]);
     if (mag > s->f_limit) s->fv[i] = s->fv[i] * (s->f_limit / mag);
+    V3 f = s->fv[i];
+    if (i < (int)s->frep_cell.size()) f += s->frep_cell[i];
+    if (i < (int)s->frep_wall.size()) f += s->frep_wall[i];
     for (const auto& pr : s->kern[i]) {
-      s->F[0 * N + pr.first] += s->fv[i].x * pr.second;
-      s->F[1 * N + pr.first] += s->fv[i].y * pr.second;
-      s->F[2 * N + pr.first] += s->fv[i].z * pr.second;
+      s->F[0 * N + pr.first] += f.x * pr.second;
+      s->F[1 * N + pr.first] += f.y * pr.second;
+      s->F[2 * N + pr.first] += f.z * pr.second;
     }
   }
+}
+
+// Node of a position, int(x + 0.5) per axis (core/hemoCellParticleField.cpp:153-156),
+// wrapped on periodic axes; false when it lies outside a bounded axis.
+bool binNode(const orc_sim* s, const V3& p, long q[3]) {
+  const double c[3] = {p.x, p.y, p.z};
+  const long n[3] = {s->nx, s->ny, s->nz};
+  for (int a = 0; a < 3; ++a) {
+    long v = (long)std::floor(c[a] + 0.5);
+    if (s->per[a]) v = ((v % n[a]) + n[a]) % n[a];
+    else if (v < 0 || v >= n[a]) return false;
+    q[a] = v;
+  }
+  return true;
+}
+
+// Separation a - b under the minimum-image convention on periodic axes.
+V3 separation(const orc_sim* s, V3 d) {
+  double c[3] = {d.x, d.y, d.z};
+  const double n[3] = {(double)s->nx, (double)s->ny, (double)s->nz};
+  for (int a = 0; a < 3; ++a)
+    if (s->per[a]) c[a] -= n[a] * std::floor(c[a] / n[a] + 0.5);
+  return {c[0], c[1], c[2]};
+}
+
+// applyRepulsionForce, core/hemoCellParticleField.cpp:677-743: vertices are
+// binned per node; each node is paired with itself and its 13 forward
+// neighbours, and every pair of vertices of different cells closer than the
+// cutoff repels with r_const * (cutoff / d) along the separation (+ on the
+// first, - on the second).  A node paired with itself visits each pair in both
+// orders, so pairs sharing a node count twice, as in the reference.
+void repulsionCells(orc_sim* s) {
+  const int V = (int)s->x.size();
+  s->frep_cell.assign(V, {0, 0, 0});
+  std::map<long, std::vector<int>> grid;
+  for (int i = 0; i < V; ++i) {
+    if (!s->cells[s->vcell[i]].alive) continue;
+    long q[3];
+    if (binNode(s, s->x[i], q)) grid[s->idx(q[0], q[1], q[2])].push_back(i);
+  }
+  static const int D[14][3] = {{0, 0, 0},  {0, 1, 0},  {0, 0, 1},   {0, 1, 1},  {1, 0, 0},
+                               {1, 1, 0},  {1, 0, 1},  {1, 1, 1},   {1, 0, -1}, {1, -1, 0},
+                               {1, -1, -1}, {1, 1, -1}, {1, -1, 1}, {0, 1, -1}};
+  const double rc = s->rep_cutoff, rk = s->rep_const;
+  for (const auto& cell : grid) {
+    const long n = cell.first;
+    const long X = n % s->nx, Y = (n / s->nx) % s->ny, Z = n / ((long)s->nx * s->ny);
+    for (const auto& d : D) {
+      long q[3] = {X + d[0], Y + d[1], Z + d[2]};
+      const long dims[3] = {s->nx, s->ny, s->nz};
+      bool out = false;
+      for (int a = 0; a < 3; ++a) {
+        if (q[a] < 0 || q[a] >= dims[a]) {
+          if (s->per[a]) q[a] = (q[a] + dims[a]) % dims[a];
+          else out = true;
+        }
+      }
+      if (out) continue;
+      const auto it = grid.find(s->idx(q[0], q[1], q[2]));
+      if (it == grid.end()) continue;
+      for (int pi : cell.second)
+        for (int qi : it->second) {
+          if (pi == qi || s->vcell[pi] == s->vcell[qi]) continue;
+          const V3 dv = separation(s, s->x[pi] - s->x[qi]);
+          const double dist = norm(dv);
+          if (dist < rc) {
+            const V3 rfm = dv * (rk * (rc / dist) / dist);
+            s->frep_cell[pi] += rfm;
+            s->frep_cell[qi] = s->frep_cell[qi] - rfm;
+          }
+        }
+    }
+  }
+}
+
+// populateBoundaryParticles, core/hemoCellParticleField.cpp:865-889: wall
+// nodes with a fluid node among their 26 neighbours.
+void findBoundaryNodes(orc_sim* s) {
+  s->boundary_nodes.clear();
+  const long dims[3] = {s->nx, s->ny, s->nz};
+  for (long Z = 0; Z < s->nz; ++Z)
+    for (long Y = 0; Y < s->ny; ++Y)
+      for (long X = 0; X < s->nx; ++X) {
+        if (s->flag[s->idx(X, Y, Z)] == 0) continue;
+        bool near_fluid = false;
+        for (int dz = -1; dz <= 1 && !near_fluid; ++dz)
+          for (int dy = -1; dy <= 1 && !near_fluid; ++dy)
+            for (int dx = -1; dx <= 1 && !near_fluid; ++dx) {
+              long q[3] = {X + dx, Y + dy, Z + dz};
+              bool out = false;
+              for (int a = 0; a < 3; ++a)
+                if (q[a] < 0 || q[a] >= dims[a]) {
+                  if (s->per[a]) q[a] = (q[a] + dims[a]) % dims[a];
+                  else out = true;
+                }
+              if (!out && s->flag[s->idx(q[0], q[1], q[2])] == 0) near_fluid = true;
+            }
+        if (near_fluid) s->boundary_nodes.push_back(s->idx(X, Y, Z));
+      }
+}
+
+// applyBoundaryRepulsionForce, core/hemoCellParticleField.cpp:891-918: a
+// vertex binned within one node of a boundary node b and closer than the
+// cutoff is pushed away from b with br_const * (cutoff / d).
+void repulsionWalls(orc_sim* s) {
+  const int V = (int)s->x.size();
+  s->frep_wall.assign(V, {0, 0, 0});
+  std::vector<char> is_b(s->N, 0);
+  for (long b : s->boundary_nodes) is_b[b] = 1;
+  const double rc = s->brep_cutoff, rk = s->brep_const;
+  const long dims[3] = {s->nx, s->ny, s->nz};
+  for (int i = 0; i < V; ++i) {
+    if (!s->cells[s->vcell[i]].alive) continue;
+    long q0[3];
+    if (!binNode(s, s->x[i], q0)) continue;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          long q[3] = {q0[0] + dx, q0[1] + dy, q0[2] + dz};
+          bool out = false;
+          for (int a = 0; a < 3; ++a)
+            if (q[a] < 0 || q[a] >= dims[a]) {
+              if (s->per[a]) q[a] = (q[a] + dims[a]) % dims[a];
+              else out = true;
+            }
+          if (out || !is_b[s->idx(q[0], q[1], q[2])]) continue;
+          const V3 dv = separation(s, s->x[i] - V3{(double)q[0], (double)q[1], (double)q[2]});
+          const double dist = norm(dv);
+          if (dist < rc) s->frep_wall[i] += dv * (rk * (rc / dist) / dist);
+        }
+  }
+}
+
+// The repulsion terms due at this step (core/hemoCell.cpp:307-312).  Each
+// term is recomputed at its own timescale and kept in between.
+void repulsion(orc_sim* s) {
+  if (s->rep_every > 0 && s->iter % s->rep_every == 0) repulsionCells(s);
+  if (s->brep_every > 0 && s->iter % s->brep_every == 0) repulsionWalls(s);
 }
 
 // interpolateFluidVelocity, core/hemoCellParticleField.cpp:819-839, with the
@@ -824,6 +971,37 @@ void orc_set_vertex_forces(orc_sim* s, int n, const int* ids, const double* forc
   for (int k = 0; k < n; ++k) s->ext.push_back({ids[k], V3{forces[3 * k], forces[3 * k + 1], forces[3 * k + 2]}});
 }
 
+// setRepulsion / enableBoundaryParticles (core/hemoCell.cpp:420-436); cutoffs
+// in lattice units, every <= 0 disables the term
+void orc_set_repulsion(orc_sim* s, double k, double cutoff, int every) {
+  s->rep_const = k;
+  s->rep_cutoff = cutoff;
+  s->rep_every = every > 0 ? every : 0;
+  if (s->rep_every == 0) s->frep_cell.clear();
+}
+void orc_set_boundary_repulsion(orc_sim* s, double k, double cutoff, int every) {
+  s->brep_const = k;
+  s->brep_cutoff = cutoff;
+  s->brep_every = every > 0 ? every : 0;
+  if (s->brep_every == 0) s->frep_wall.clear();
+  else findBoundaryNodes(s);
+}
+void orc_stage_repulsion(orc_sim* s) {
+  if (s->rep_every > 0) repulsionCells(s);
+  if (s->brep_every > 0) repulsionWalls(s);
+}
+void orc_read_repulsion(orc_sim* s, double* f) {
+  const int V = (int)s->x.size();
+  for (int i = 0; i < V; ++i) {
+    V3 r = {0, 0, 0};
+    if (i < (int)s->frep_cell.size()) r += s->frep_cell[i];
+    if (i < (int)s->frep_wall.size()) r += s->frep_wall[i];
+    f[3 * i] = r.x;
+    f[3 * i + 1] = r.y;
+    f[3 * i + 2] = r.z;
+  }
+}
+
 void orc_stage_spread(orc_sim* s) { spread(s); }
 void orc_stage_collide_stream(orc_sim* s) {
   collideStream(s);
@@ -833,10 +1011,11 @@ void orc_stage_interpolate(orc_sim* s) { interpolate(s); }
 void orc_stage_advance(orc_sim* s) { advance(s); }
 void orc_stage_mechanics(orc_sim* s, int forced) { mechanics(s, forced != 0); }
 
-// HemoCell::iterate, core/hemoCell.cpp:299-376 (repulsion, CEPAC, solidify
-// and interior viscosity are not part of this path).
+// HemoCell::iterate, core/hemoCell.cpp:299-376 (CEPAC, solidify and
+// interior viscosity are not part of this path).
 void orc_step(orc_sim* s, int nsteps) {
   for (int k = 0; k < nsteps; ++k) {
+    repulsion(s);
     spread(s);
     collideStream(s);
     resetForce(s);

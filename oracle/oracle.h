@@ -67,6 +67,10 @@ void orc_set_vertex_forces(orc_sim* s, int n, const int* ids, const double* forc
 
 /* Stepping --------------------------------------------------------------- */
 void orc_step(orc_sim* s, int nsteps);
+void orc_set_repulsion(orc_sim* s, double k, double cutoff, int every);
+void orc_set_boundary_repulsion(orc_sim* s, double k, double cutoff, int every);
+void orc_stage_repulsion(orc_sim* s);
+void orc_read_repulsion(orc_sim* s, double* f); /* [V][3] */
 void orc_stage_spread(orc_sim* s);
 void orc_stage_collide_stream(orc_sim* s); /* + force reset, keeping the old field */
 void orc_stage_interpolate(orc_sim* s);

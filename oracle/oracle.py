@@ -34,6 +34,10 @@ _SIG = {
     "orc_set_timescales": (None, [P, I, C.c_int]),
     "orc_set_vertex_forces": (None, [P, C.c_int, I, D]),
     "orc_step": (None, [P, C.c_int]),
+    "orc_set_repulsion": (None, [P, C.c_double, C.c_double, C.c_int]),
+    "orc_set_boundary_repulsion": (None, [P, C.c_double, C.c_double, C.c_int]),
+    "orc_stage_repulsion": (None, [P]),
+    "orc_read_repulsion": (None, [P, D]),
     "orc_stage_spread": (None, [P]),
     "orc_stage_collide_stream": (None, [P]),
     "orc_stage_interpolate": (None, [P]),
@@ -152,11 +156,24 @@ class Oracle:
         forces = np.ascontiguousarray(forces, np.float64).reshape(-1, 3)
         self.L.orc_set_vertex_forces(self.s, len(ids), _i(ids), _d(forces))
 
+    def set_repulsion(self, k, cutoff_lu, every=1):
+        self.L.orc_set_repulsion(self.s, float(k), float(cutoff_lu), int(every))
+
+    def set_boundary_repulsion(self, k, cutoff_lu, every=1):
+        self.L.orc_set_boundary_repulsion(self.s, float(k), float(cutoff_lu), int(every))
+
+    def read_repulsion(self):
+        f = np.zeros((self.nvertices(), 3))
+        self.L.orc_read_repulsion(self.s, _d(f))
+        return f
+
     def step(self, n=1):
         self.L.orc_step(self.s, n)
 
     def stage(self, name, forced=1):
-        if name == "mechanics":
+        if name == "repulsion":
+            self.L.orc_stage_repulsion(self.s)
+        elif name == "mechanics":
             self.L.orc_stage_mechanics(self.s, forced)
         else:
             getattr(self.L, "orc_stage_" + name)(self.s)

@@ -35,9 +35,11 @@ SHEAR_FILE = os.path.join(HERE, "shear_rbc_50_1000.npz")
 PIPE_FILE = os.path.join(HERE, "pipe_ht25_2000.npz")
 
 
-def sample_nodes(N: int) -> np.ndarray:
-    """About 2000 nodes spread over the lattice (odd stride)."""
-    return np.arange(0, N, (N // 2000) | 1)
+def sample_nodes(N: int, fluid: np.ndarray) -> np.ndarray:
+    """About 2000 nodes spread over the lattice (odd stride), fluid only: the
+    density and velocity of a wall node are not part of the solution."""
+    idx = np.arange(0, N, (N // 2000) | 1)
+    return idx[fluid[idx]]
 
 
 def stage_dumps(threads: int = 0) -> dict:
@@ -54,7 +56,7 @@ def stage_dumps(threads: int = 0) -> dict:
     out["spread_F"] = F[:, nz]
     o.stage("collide_stream")
     rho, u = o.read_fluid()
-    idx = sample_nodes(case.N)
+    idx = sample_nodes(case.N, case.flags_array() == 0)
     out["collide_rho"] = rho[idx]
     out["collide_u"] = u[:, idx]
     o.stage("interpolate")
@@ -95,7 +97,7 @@ def run_summary(case, o, positions: bool = True) -> dict:
     nvs = [xyz.shape[0] for _, xyz in case.cells]
     offs = np.concatenate([[0], np.cumsum(nvs)])
     centroids = np.array([x[offs[c]:offs[c + 1]].mean(axis=0) for c in range(len(nvs))])
-    idx = sample_nodes(case.N)
+    idx = sample_nodes(case.N, fluid)
     out = dict(alive=alive, volume=vol, centroids=centroids,
                u_plane=uf.sum(axis=(2, 3)) / np.maximum(cnt.sum(axis=(1, 2)), 1),
                u_column=uf.sum(axis=1) / np.maximum(cnt.sum(axis=0), 1),

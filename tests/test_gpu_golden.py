@@ -25,7 +25,7 @@ def _summary(case, hc, positions=True):
     nvs = [xyz.shape[0] for _, xyz in case.cells]
     offs = np.concatenate([[0], np.cumsum(nvs)])
     g = _gen()
-    idx = g.sample_nodes(case.N)
+    idx = g.sample_nodes(case.N, fluid)
     out = dict(alive=alive, volume=vol,
                centroids=np.array([x[offs[c]:offs[c + 1]].mean(axis=0) for c in range(len(nvs))]),
                u_plane=uf.sum(axis=(2, 3)) / np.maximum(cnt.sum(axis=(1, 2)), 1),

@@ -64,6 +64,114 @@ def test_collide_stream_one_stage(built):
     hc.close()
 
 
+def _k1_codes():
+    # bulk collide-stream: stages | CTAs per SM << 4
+    return [3 | (1 << 4), 4 | (2 << 4), 2 | (3 << 4)]
+
+
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("code", _k1_codes())
+@pytest.mark.parametrize("wall", [True, False])
+def test_collide_stream_bulk_matches_direct(built, form, code, wall):
+    """The bulk-copy collide-stream gives the same bits as the direct pull,
+    with moving walls (bounce-back, y/z edges) and fully periodic."""
+    case = mixed_box(wall=wall)
+    a = case.build(form=form)
+    b = case.build(form=form)
+    o = _orc().apply_case(case)
+    randomize(case, a, o)
+    randomize(case, b, o)
+    t = b.tuning()
+    t[7] = code
+    b.set_tuning(t)
+    a.stage(1)
+    b.stage(1)
+    assert np.array_equal(a.read_populations(), b.read_populations())
+    assert np.array_equal(a.read_force_field(0), b.read_force_field(0))
+    assert b.device_status() == 0
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_bulk_collide_stream_full_steps(built, form):
+    """Whole steps with the bulk collide-stream, batched and graph-replayed,
+    against the direct collide-stream: FP64 within the run tolerance, FP32
+    within 1e-5 (the spread's float atomics may add in another order)."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=True)
+    a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    t = b.tuning()
+    t[7] = 4 | (1 << 4)
+    b.set_tuning(t)
+    a.iterate(60)
+    b.iterate(60)
+    tol = RUN_TOL if form == 0 else 1e-5
+    assert rel_l2(b.read_vertices()[0], a.read_vertices()[0]) < tol
+    assert rel_l2(b.read_fluid()[1], a.read_fluid()[1]) < tol
+    # the same cells reach the walls in both; no pipeline wait ran out
+    assert b.device_status() == a.device_status() and (b.device_status() & 4) == 0
+    a.close()
+    b.close()
+
+
+def test_bulk_collide_stream_rejects_unsuitable_lattice(built):
+    from hemocell_gb300.hemocell import HemoCellError
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    case = C.shear_single_rbc(n=50, shear_rate=100.0, seed=1)   # 50 floats per row: not 16-byte rows
+    hc = case.build(form=L.HC_FORM_MIXED_F32)
+    t = hc.tuning()
+    t[7] = 4 | (1 << 4)
+    with pytest.raises(HemoCellError):
+        hc.set_tuning(t)
+    hc.close()
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_repulsion_stage(built, form):
+    """applyRepulsionForce + applyBoundaryRepulsionForce against the oracle:
+    FP64 within the stage tolerance, FP32 within 1e-5."""
+    from hemocell_gb300 import _lib as L
+    case = _cases().repulsion_box()
+    hc = case.build(form=form)
+    o = _orc().apply_case(case)
+    hc._check(hc._lib.hc_set_repulsion(hc._h, 1e-4, 2.0, 1))
+    hc._check(hc._lib.hc_set_boundary_repulsion(hc._h, 5e-5, 2.0, 1))
+    o.set_repulsion(1e-4, 2.0, 1)
+    o.set_boundary_repulsion(5e-5, 2.0, 1)
+    hc.stage(L.HC_STAGE_REPULSION)
+    o.stage("repulsion")
+    fg, fo = hc.read_repulsion(), o.read_repulsion()
+    assert np.count_nonzero(np.any(fo != 0, axis=1)) > 50
+    assert rel_l2(fg, fo) < (STAGE_TOL if form == 0 else 1e-5)
+    assert hc.device_status() == 0
+    hc.close()
+
+
+@pytest.mark.parametrize("launch", [0, 1])
+def test_repulsion_full_steps(built, launch):
+    """Whole FP64 steps with both repulsion terms (per stage, and batched with
+    the fused spread) against the oracle after 60 steps."""
+    case = _cases().repulsion_box()
+    hc = case.build(launch=launch)
+    o = _orc().apply_case(case)
+    hc.setRepulsion(1e-4, 1.0)                 # micrometres: 2 lattice units
+    hc.enableBoundaryParticles(5e-5, 1.0)
+    o.set_repulsion(1e-4, 2.0, 1)
+    o.set_boundary_repulsion(5e-5, 2.0, 1)
+    hc.iterate(60)
+    o.step(60)
+    xg, vg, _ = hc.read_vertices()
+    xo, vo, _ = o.read_vertices()
+    assert rel_l2(xg, xo) < RUN_TOL
+    assert rel_l2(vg, vo) < RUN_TOL
+    fluid = case.flags_array() == 0
+    assert rel_l2(hc.read_fluid()[1][:, fluid], o.read_fluid()[1][:, fluid]) < RUN_TOL
+    hc.close()
+
+
 def test_fluid_only_shear_100_steps(built):
     C = _cases()
     n = (16, 12, 20)

@@ -150,3 +150,24 @@ def test_ring_and_edges_consistent(orc):
     assert abs(vol_eq - cases.mesh_volume(spec.mesh)) < 1e-9 * vol_eq
     assert abs(area_mean - k["tri_a0"].mean()) < 1e-12
     assert abs(edge_mean - k["edge_l0"].mean()) < 1e-12
+
+
+def test_repulsion_conserves_momentum_and_pushes_from_walls(built):
+    """Inter-cell repulsion is pairwise equal and opposite (its sum vanishes);
+    the wall term pushes the lower cell up, away from the bottom wall."""
+    from hemocell_gb300 import cases
+    from oracle import oracle as orc
+    case = cases.repulsion_box()
+    o = orc.apply_case(case)
+    o.set_repulsion(1e-4, 2.0, 1)
+    o.stage("repulsion")
+    f = o.read_repulsion()
+    assert np.count_nonzero(np.any(f != 0, axis=1)) > 50
+    assert np.abs(f.sum(axis=0)).max() < 1e-12 * np.abs(f).sum()
+    nv = case.cells[0][1].shape[0]
+    assert f[:nv, 2].sum() < 0 < f[nv:, 2].sum()    # the stacked cells push apart
+    w = orc.apply_case(case)
+    w.set_boundary_repulsion(5e-5, 2.0, 1)
+    w.stage("repulsion")
+    fw = w.read_repulsion()
+    assert fw[:nv, 2].sum() > 0 and np.all(fw[nv:] == 0)
