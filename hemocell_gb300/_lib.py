@@ -101,6 +101,10 @@ SIGNATURES = {
     "hc_read_cells": (C.c_int, [P, I, D]),
     "hc_read_bins": (C.c_int, [P, I, I, I, I, I, I, C.c_int]),
     "hc_bin_tiles_noalloc": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P, P, C.c_int, P]),
+    "hc_cell_info": (C.c_int, [P, D]),
+    "hc_write_cell_info_csv": (C.c_int, [P, C.c_char_p, C.c_int]),
+    "hc_save_checkpoint": (C.c_int, [P, C.c_char_p]),
+    "hc_load_checkpoint": (C.c_int, [P, C.c_char_p]),
     "hc_get_stats": (C.c_int, [P, C.POINTER(hc_stats)]),
     "hc_device_status": (C.c_int, [P, C.POINTER(C.c_uint)]),
     "hc_autotune": (C.c_int, [P, C.c_char_p]),

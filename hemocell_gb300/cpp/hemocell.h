@@ -332,6 +332,33 @@ class HemoCell {
     check(hc_set_body_force(h_, HC_BODY_UNIFORM, p));
   }
 
+  // <outputDirectory>/<checkpointDirectory>/ as config/config.cpp:168-173 sets it
+  std::string outputDirectory() const {
+    std::string out = "./tmp";
+    try {
+      out = (*cfg)["parameters"]["outputDirectory"].read<std::string>();
+    } catch (std::invalid_argument&) {
+    }
+    return out;
+  }
+  std::string checkpointDirectory() const {
+    std::string sub = "checkpoint";
+    try {
+      sub = (*cfg)["parameters"]["checkpointDirectory"].read<std::string>();
+    } catch (std::invalid_argument&) {
+    }
+    return outputDirectory() + "/" + sub + "/";
+  }
+  // core/hemoCell.cpp:210-219 and :199-208
+  void saveCheckPoint() { check(hc_save_checkpoint(h_, checkpointDirectory().c_str())); }
+  void loadCheckPoint() {
+    check(hc_load_checkpoint(h_, checkpointDirectory().c_str()));
+    hc_stats st;
+    check(hc_get_stats(h_, &st));
+    iter = (unsigned int)st.iter;
+  }
+  bool outputInSiUnits = false;
+
   // core/hemoCell.cpp:299-376
   void iterate() {
     check(hc_step(h_, 1));
@@ -373,5 +400,12 @@ class HemoCell {
     check(hc_set_timescales(h_, every.data(), (int)every.size(), (int)cellfields->particleVelocityUpdateTimescale));
   }
 };
+
+// io/writeCellInfoCSV.cpp:30-74: <outputDirectory>/csv/<type>.<iteration>.csv
+inline void writeCellInfo_CSV(HemoCell& hemocell) {
+  const std::string dir = hemocell.outputDirectory() + "/csv";
+  if (hc_write_cell_info_csv(hemocell.handle(), dir.c_str(), hemocell.outputInSiUnits ? 1 : 0) != HC_OK)
+    die(std::string("(writeCellInfo_CSV) ") + hc_last_error(hemocell.handle()));
+}
 
 }  // namespace hemo

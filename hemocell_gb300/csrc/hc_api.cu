@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <functional>
 #include <map>
@@ -109,6 +110,10 @@ struct hc_handle {
   void* frep_cell = nullptr;
   void* frep_wall = nullptr;
   long long rep_vcap = 0;
+  // fluid nodes in lattice order, packed (collide-stream and node velocity over them)
+  uint32_t* fluid = nullptr;
+  int nfluid = 0;
+  long long fluid_cap = 0;
   // bulk-copy collide-stream plan for tune[7] (stages | CTAs per SM << 4)
   hcd::BulkPlan bulk{};
   int bulk_key = 0;
@@ -232,6 +237,8 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
   L.status = h->status;
+  L.fluid = h->nfluid > 0 ? h->fluid : nullptr;
+  L.nfluid = h->nfluid;
   L.fast = 19LL * h->N < (1LL << 31) ? 1 : 0;
   const long long nxy = (long long)h->nx * h->ny;
   for (int j = 0; j < 19; ++j)
@@ -307,6 +314,27 @@ int upload_flags(hc_handle* h) {
   build_nbmask(h, mask);
   HC_CUDA(h, cudaMemcpyAsync(h->flag, h->hflag.data(), h->N, cudaMemcpyHostToDevice, h->stream));
   HC_CUDA(h, cudaMemcpyAsync(h->nbmask, mask.data(), 4 * h->N, cudaMemcpyHostToDevice, h->stream));
+  // the fluid-node list, when coordinates pack into 10/10/12 bits and every
+  // population index fits 32 bits
+  std::vector<uint32_t> fl;
+  if (h->nx <= 1024 && h->ny <= 1024 && h->nz <= 4096 && 19LL * h->N < (1LL << 31)) {
+    fl.reserve(h->N);
+    for (int Z = 0; Z < h->nz; ++Z)
+      for (int Y = 0; Y < h->ny; ++Y)
+        for (int X = 0; X < h->nx; ++X)
+          if (h->hflag[X + (long long)h->nx * (Y + (long long)h->ny * Z)] == 0)
+            fl.push_back((uint32_t)X | ((uint32_t)Y << 10) | ((uint32_t)Z << 20));
+    if ((long long)fl.size() > h->fluid_cap) {
+      dfree(h, h->fluid);
+      h->fluid = nullptr;
+      h->device_bytes -= 4 * h->fluid_cap;
+      h->fluid_cap = 0;
+      HC_CUDA(h, dalloc(h, (void**)&h->fluid, 4 * std::max<size_t>(fl.size(), 1)));
+      h->fluid_cap = (long long)std::max<size_t>(fl.size(), 1);
+    }
+    if (!fl.empty()) HC_CUDA(h, cudaMemcpyAsync(h->fluid, fl.data(), 4 * fl.size(), cudaMemcpyHostToDevice, h->stream));
+  }
+  h->nfluid = (int)fl.size();
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   return HC_OK;
 }
@@ -477,8 +505,16 @@ int enq_spread(hc_handle* h) {
 
 template <typename T>
 cudaError_t launch_k1(hc_handle* h, const LbmView<T>& L) {
-  if (h->tune[7] != 0 && h->bulk_key == h->tune[7]) return hcd::launch_collide_stream_bulk<T>(L, h->bulk, h->stream);
+  const int mode = h->tune[7] & 0xff;
+  if (mode == 1 && L.fluid) return hcd::launch_collide_stream_fluid<T>(L, h->tune[0], h->stream);
+  if (mode >= 2 && h->bulk_key == mode) return hcd::launch_collide_stream_bulk<T>(L, h->bulk, h->stream);
   return hcd::launch_collide_stream<T>(L, h->tune[0], h->tune[1], h->stream);
+}
+
+template <typename T>
+cudaError_t launch_nv(hc_handle* h, const LbmView<T>& L) {
+  if ((h->tune[7] & 0x100) && L.fluid) return hcd::launch_node_velocity_fluid<T>(L, h->stream);
+  return hcd::launch_node_velocity<T>(L, h->stream);
 }
 
 template <typename T>
@@ -494,7 +530,8 @@ int enq_collide(hc_handle* h) {
 // does not allow that configuration.
 template <typename T>
 bool set_bulk_plan(hc_handle* h, int code) {
-  if (code == 0) return true;
+  code &= 0xff;
+  if (code < 2) return true;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
   hcd::BulkPlan P;
@@ -513,7 +550,7 @@ int enq_interp_advance(hc_handle* h, int do_interp, int do_advance, int mark = 0
   LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
   if (do_interp) {
     if (mark) HC_CUDA(h, hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream));
-    HC_CUDA(h, hcd::launch_node_velocity<T>(L, h->stream));
+    HC_CUDA(h, launch_nv<T>(h, L));
   }
   HC_CUDA(h, hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, do_interp, do_advance, h->tune[3],
                                            h->stream));
@@ -820,7 +857,7 @@ float time_it(hc_handle* h, int reps, int which) {
     } else if (which == 1) {
       LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
       hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream);
-      hcd::launch_node_velocity<T>(L, h->stream);
+      launch_nv<T>(h, L);
       hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, 1, 0, h->tune[3], h->stream);
     } else {
       enq_mechanics<T>(h, true);
@@ -888,11 +925,26 @@ int autotune(hc_handle* h, const char* cache) {
   }
   h->tune[0] = bx;
   h->tune[1] = by;
-  // bulk-copy variant: stages x CTAs per SM
+  // one thread per fluid node, and the bulk-copy variant (stages x CTAs per SM)
   int b7 = 0;
   h->tune[7] = 0;
+  if (h->nfluid > 0)
+    for (int bs : {128, 256}) {
+      const int keep0 = h->tune[0];
+      h->tune[0] = bs;
+      h->tune[7] = 1;
+      float t = time_it<T>(h, 5, 0);
+      if (t < best) {
+        best = t;
+        b7 = 1;
+        bx = bs;
+        by = 1;
+      }
+      h->tune[0] = keep0;
+      h->tune[7] = 0;
+    }
   for (int ctas : {1, 2})
-    for (int st : {3, 4, 6}) {
+    for (int st : {3, 4}) {
       const int code = st | (ctas << 4);
       if (!set_bulk_plan<T>(h, code)) continue;
       h->tune[7] = code;
@@ -903,20 +955,29 @@ int autotune(hc_handle* h, const char* cache) {
       }
       h->tune[7] = 0;
     }
+  h->tune[0] = bx;
+  h->tune[1] = by;
   h->tune[7] = b7;
-  if (b7 != 0) set_bulk_plan<T>(h, b7);
+  if (b7 >= 2) set_bulk_plan<T>(h, b7);
   if (h->nvert > 0) {
     best = 1e30f;
     int bb = h->tune[3];
-    for (int bs : {64, 128, 256}) {
-      h->tune[3] = bs;
-      float t = time_it<T>(h, 5, 1);
-      if (t < best) {
-        best = t;
-        bb = bs;
+    const int k7 = h->tune[7] & 0xff;
+    int nvf = 0;
+    for (int fl : {0, 0x100})
+      for (int bs : {64, 128, 256}) {
+        if (fl && h->nfluid == 0) continue;
+        h->tune[3] = bs;
+        h->tune[7] = k7 | fl;
+        float t = time_it<T>(h, 5, 1);
+        if (t < best) {
+          best = t;
+          bb = bs;
+          nvf = fl;
+        }
       }
-    }
     h->tune[3] = bb;
+    h->tune[7] = k7 | nvf;
     h->tune[2] = bb;
     best = 1e30f;
     int mb = h->tune[4], mg = h->tune[5], mv = h->tune[6];
@@ -1122,7 +1183,7 @@ int hc_destroy(hc_handle* h) {
                   h->alive,  h->dcells_all, h->status, h->bin_counts, h->bin_cursor, h->bin_offsets,
                   h->tile_vertices, h->tile_cell_counts, h->tile_cell_offsets, h->tile_cells, h->scratch,
                   h->ext_ids, h->ext_f, h->rep_cnt, h->rep_slot, h->rep_vq, h->rep_xr, h->rep_bnode,
-                  h->frep_cell, h->frep_wall};
+                  h->frep_cell, h->frep_wall, h->fluid};
   for (void* q : ptrs) dfree(h, q);
   if (h->pool) release_pool(h->p.device, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1691,15 +1752,286 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
   if (in8[4] <= 0 || in8[4] > (h->f64 ? 384 : 768) || in8[4] % 32 != 0)
     return fail(h, HC_ERR_INVALID, "bad mechanics block size");
   if (in8[6] != 0 && in8[6] != 1) return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather) or 1 (scatter)");
-  if (in8[7] != 0) {
-    const int st = in8[7] & 15, ctas = in8[7] >> 4;
-    if (st < 2 || st > 8 || ctas < 1 || ctas > 4)
-      return fail(h, HC_ERR_INVALID, "bulk collide-stream code is stages (2-8) | CTAs per SM (1-4) << 4");
-    const bool ok = h->f64 ? set_bulk_plan<double>(h, in8[7]) : set_bulk_plan<float>(h, in8[7]);
-    if (!ok) return fail(h, HC_ERR_INVALID, "the lattice does not allow the bulk collide-stream (row bytes, rows, shared memory)");
+  {
+    const int mode = in8[7] & 0xff;
+    if ((in8[7] & ~0x1ff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-8 are defined");
+    if ((mode == 1 || (in8[7] & 0x100)) && h->nfluid == 0)
+      return fail(h, HC_ERR_INVALID, "no fluid-node list for this lattice");
+    if (mode >= 2) {
+      const int st = mode & 15, ctas = mode >> 4;
+      if (st < 2 || st > 8 || ctas < 1 || ctas > 4)
+        return fail(h, HC_ERR_INVALID, "bulk collide-stream code is stages (2-8) | CTAs per SM (1-4) << 4");
+      const bool ok = h->f64 ? set_bulk_plan<double>(h, mode) : set_bulk_plan<float>(h, mode);
+      if (!ok) return fail(h, HC_ERR_INVALID, "the lattice does not allow the bulk collide-stream (row bytes, rows, shared memory)");
+    }
   }
   std::memcpy(h->tune, in8, sizeof(h->tune));
   invalidate_graph(h);
+  return HC_OK;
+}
+
+// ---- cell information and CSV output --------------------------------------
+int hc_cell_info(hc_handle* h, double* out) {
+  if (!h || !out) return HC_ERR_INVALID;
+  const int C = h->ncells;
+  if (C == 0) return HC_OK;
+  int rc;
+  if ((rc = ensure_scratch(h, sizeof(double) * 16 * (size_t)C)) != HC_OK) return rc;
+  if (h->f64)
+    HC_CUDA(h, hcd::launch_cell_info<double>(vertex_view<double>(h), h->cell_type, h->cell_voff, h->dtypes, C,
+                                             h->scratch, h->stream));
+  else
+    HC_CUDA(h, hcd::launch_cell_info<float>(vertex_view<float>(h), h->cell_type, h->cell_voff, h->dtypes, C,
+                                            h->scratch, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(out, h->scratch, sizeof(double) * 16 * (size_t)C, cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  // centroids are reported inside the lattice on periodic axes
+  const int n[3] = {h->nx, h->ny, h->nz};
+  for (int c = 0; c < C; ++c)
+    for (int a = 0; a < 3; ++a)
+      if (h->p.periodic[a]) out[16 * c + a] -= n[a] * std::floor(out[16 * c + a] / n[a]);
+  return HC_OK;
+}
+
+int hc_write_cell_info_csv(hc_handle* h, const char* dir, int si) {
+  if (!h || !dir) return HC_ERR_INVALID;
+  std::vector<double> info(16 * (size_t)h->ncells);
+  int rc;
+  if ((rc = hc_cell_info(h, info.data())) != HC_OK) return rc;
+  std::error_code ec;
+  std::filesystem::create_directories(dir, ec);
+  if (ec) return fail(h, HC_ERR_INVALID, "cannot create " + std::string(dir) + ": " + ec.message());
+  char iter[32];
+  std::snprintf(iter, sizeof iter, "%012d", h->iter);
+  const double dx = h->p.dx, dt = h->p.dt;
+  for (size_t ty = 0; ty < h->types.size(); ++ty) {
+    const std::string path = std::string(dir) + "/" + h->types[ty].name + "." + iter + ".csv";
+    std::ofstream out(path, std::ios::trunc);
+    if (!out) return fail(h, HC_ERR_INVALID, "cannot write " + path);
+    out << "X,Y,Z,area,volume,atomic_block,cellId,baseCellId,velocity_x,velocity_y,velocity_z\n";
+    out.precision(17);
+    for (int c = 0; c < h->ncells; ++c) {
+      const double* r = info.data() + 16 * (size_t)c;
+      if ((int)r[15] != (int)ty) continue;  // other type, or deleted
+      const double lp = si ? dx : 1.0, la = si ? dx * dx : 1.0, lv = si ? dx * dx * dx : 1.0,
+                   lu = si ? dx / dt : 1.0;
+      out << r[0] * lp << "," << r[1] * lp << "," << r[2] * lp << "," << r[6] * la << "," << r[7] * lv << ",0,"
+          << c << "," << c << "," << r[3] * lu << "," << r[4] * lu << "," << r[5] * lu << "\n";
+    }
+  }
+  return HC_OK;
+}
+
+// ---- checkpoints ------------------------------------------------------------
+namespace {
+
+struct LatticeHeader {
+  char magic[8];
+  int32_t version, nx, ny, nz, ts, cur, iter, body_mode;
+  double body[3];
+  double uw[hcd::MAX_WALL_CLASSES][3];
+};
+
+struct ParticleHeader {
+  char magic[8];
+  int32_t version, ts, ntypes, ncells, nvert, has_frep_cell, has_frep_wall;
+  int32_t nv[hcd::MAX_TYPES];
+};
+
+const char kLatMagic[8] = {'H', 'C', 'G', 'B', 'L', 'A', 'T', '1'};
+const char kParMagic[8] = {'H', 'C', 'G', 'B', 'P', 'A', 'R', '1'};
+
+int put_device(hc_handle* h, std::ofstream& out, const void* d, size_t bytes) {
+  std::vector<char> buf(std::min<size_t>(bytes, (size_t)64 << 20));
+  for (size_t off = 0; off < bytes; off += buf.size()) {
+    const size_t n = std::min(buf.size(), bytes - off);
+    HC_CUDA(h, cudaMemcpyAsync(buf.data(), (const char*)d + off, n, cudaMemcpyDeviceToHost, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+    out.write(buf.data(), (std::streamsize)n);
+  }
+  return out ? HC_OK : fail(h, HC_ERR_INVALID, "checkpoint write failed");
+}
+
+int get_device(hc_handle* h, std::ifstream& in, void* d, size_t bytes) {
+  std::vector<char> buf(std::min<size_t>(bytes, (size_t)64 << 20));
+  for (size_t off = 0; off < bytes; off += buf.size()) {
+    const size_t n = std::min(buf.size(), bytes - off);
+    in.read(buf.data(), (std::streamsize)n);
+    if (!in) return fail(h, HC_ERR_INVALID, "checkpoint file is truncated");
+    HC_CUDA(h, cudaMemcpyAsync((char*)d + off, buf.data(), n, cudaMemcpyHostToDevice, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  return HC_OK;
+}
+
+// [3][Vcap] device array: the first nvert entries of each component
+int put_soa(hc_handle* h, std::ofstream& out, const void* d, size_t es) {
+  int rc;
+  for (int a = 0; a < 3; ++a)
+    if ((rc = put_device(h, out, (const char*)d + a * es * h->Vcap, es * h->nvert)) != HC_OK) return rc;
+  return HC_OK;
+}
+int get_soa(hc_handle* h, std::ifstream& in, void* d, size_t es) {
+  int rc;
+  for (int a = 0; a < 3; ++a)
+    if ((rc = get_device(h, in, (char*)d + a * es * h->Vcap, es * h->nvert)) != HC_OK) return rc;
+  return HC_OK;
+}
+
+}  // namespace
+
+int hc_save_checkpoint(hc_handle* h, const char* dir) {
+  if (!h || !dir) return HC_ERR_INVALID;
+  int rc;
+  // a canonical state: the next step's force field holds the body force only
+  if ((rc = undo_fused_spread(h)) != HC_OK) return rc;
+  namespace fs = std::filesystem;
+  std::error_code ec;
+  fs::create_directories(dir, ec);
+  if (ec) return fail(h, HC_ERR_INVALID, "cannot create " + std::string(dir) + ": " + ec.message());
+  const std::string d = std::string(dir) + "/";
+  for (const char* f : {"lattice.dat", "particleField.dat", "checkpoint.xml"})
+    if (fs::exists(d + f)) fs::rename(d + f, d + f + ".old", ec);
+  {
+    std::ofstream out(d + "lattice.dat", std::ios::binary | std::ios::trunc);
+    if (!out) return fail(h, HC_ERR_INVALID, "cannot write " + d + "lattice.dat");
+    LatticeHeader hd;
+    std::memset(&hd, 0, sizeof hd);
+    std::memcpy(hd.magic, kLatMagic, 8);
+    hd.version = 1;
+    hd.nx = h->nx;
+    hd.ny = h->ny;
+    hd.nz = h->nz;
+    hd.ts = h->ts;
+    hd.cur = h->cur;
+    hd.iter = h->iter;
+    hd.body_mode = h->body_mode;
+    for (int a = 0; a < 3; ++a) hd.body[a] = h->body[a];
+    std::memcpy(hd.uw, h->uw, sizeof hd.uw);
+    out.write((const char*)&hd, sizeof hd);
+    out.write((const char*)h->hflag.data(), h->N);
+    if ((rc = put_device(h, out, h->f[h->cur], 19 * h->ts * (size_t)h->N)) != HC_OK) return rc;
+    const size_t Fb = h->f64 ? hcd::field_bytes<double>(h->N) : hcd::field_bytes<float>(h->N);
+    for (int k = 0; k < 2; ++k)
+      if ((rc = put_device(h, out, h->F[k], Fb)) != HC_OK) return rc;
+  }
+  {
+    std::ofstream out(d + "particleField.dat", std::ios::binary | std::ios::trunc);
+    if (!out) return fail(h, HC_ERR_INVALID, "cannot write " + d + "particleField.dat");
+    ParticleHeader hd;
+    std::memset(&hd, 0, sizeof hd);
+    std::memcpy(hd.magic, kParMagic, 8);
+    hd.version = 1;
+    hd.ts = h->ts;
+    hd.ntypes = (int)h->types.size();
+    hd.ncells = h->ncells;
+    hd.nvert = h->nvert;
+    hd.has_frep_cell = h->rep_every > 0 && h->frep_cell ? 1 : 0;
+    hd.has_frep_wall = h->brep_every > 0 && h->frep_wall ? 1 : 0;
+    for (size_t t = 0; t < h->types.size(); ++t) hd.nv[t] = h->types[t].tc.nv;
+    out.write((const char*)&hd, sizeof hd);
+    out.write((const char*)h->h_cell_type.data(), 4 * (size_t)h->ncells);
+    out.write((const char*)h->h_cell_voff.data(), 4 * (size_t)h->ncells);
+    if (h->ncells > 0 && (rc = put_device(h, out, h->alive, 4 * (size_t)h->ncells)) != HC_OK) return rc;
+    if (h->nvert > 0) {
+      if ((rc = put_soa(h, out, h->x, 8)) != HC_OK) return rc;
+      if ((rc = put_soa(h, out, h->v, h->ts)) != HC_OK) return rc;
+      if ((rc = put_soa(h, out, h->fv, h->ts)) != HC_OK) return rc;
+      if (hd.has_frep_cell && (rc = put_soa(h, out, h->frep_cell, h->ts)) != HC_OK) return rc;
+      if (hd.has_frep_wall && (rc = put_soa(h, out, h->frep_wall, h->ts)) != HC_OK) return rc;
+    }
+  }
+  std::ofstream xml(d + "checkpoint.xml", std::ios::trunc);
+  xml << "<?xml version=\"1.0\" ?>\n<Checkpoint>\n  <General>\n    <Iteration> " << h->iter
+      << " </Iteration>\n    <OutDirectory> " << dir << " </OutDirectory>\n  </General>\n  <Lattice> "
+      << h->nx << " " << h->ny << " " << h->nz << " </Lattice>\n  <Form> " << (h->f64 ? "plain_f64" : "mixed_f32")
+      << " </Form>\n  <Cells> " << h->ncells << " </Cells>\n</Checkpoint>\n";
+  return xml ? HC_OK : fail(h, HC_ERR_INVALID, "cannot write checkpoint.xml");
+}
+
+int hc_load_checkpoint(hc_handle* h, const char* dir) {
+  if (!h || !dir) return HC_ERR_INVALID;
+  int rc;
+  const std::string d = std::string(dir) + "/";
+  std::ifstream lin(d + "lattice.dat", std::ios::binary);
+  std::ifstream pin(d + "particleField.dat", std::ios::binary);
+  if (!lin || !pin) return fail(h, HC_ERR_INVALID, "no checkpoint in " + std::string(dir));
+  LatticeHeader lh;
+  lin.read((char*)&lh, sizeof lh);
+  if (!lin || std::memcmp(lh.magic, kLatMagic, 8) != 0 || lh.version != 1)
+    return fail(h, HC_ERR_INVALID, "lattice.dat is not a checkpoint of this library");
+  if (lh.nx != h->nx || lh.ny != h->ny || lh.nz != h->nz || lh.ts != h->ts)
+    return fail(h, HC_ERR_INVALID, "checkpoint lattice size or precision form differs from this handle's");
+  ParticleHeader ph;
+  pin.read((char*)&ph, sizeof ph);
+  if (!pin || std::memcmp(ph.magic, kParMagic, 8) != 0 || ph.version != 1 || ph.ts != h->ts)
+    return fail(h, HC_ERR_INVALID, "particleField.dat is not a checkpoint of this library");
+  if (ph.ntypes != (int)h->types.size()) return fail(h, HC_ERR_INVALID, "checkpoint cell types differ from this handle's");
+  for (int t = 0; t < ph.ntypes; ++t)
+    if (ph.nv[t] != h->types[t].tc.nv) return fail(h, HC_ERR_INVALID, "checkpoint cell type meshes differ");
+  std::vector<int> ctype(ph.ncells), cvoff(ph.ncells), alive(ph.ncells);
+  pin.read((char*)ctype.data(), 4 * (size_t)ph.ncells);
+  pin.read((char*)cvoff.data(), 4 * (size_t)ph.ncells);
+  pin.read((char*)alive.data(), 4 * (size_t)ph.ncells);
+  if (!pin) return fail(h, HC_ERR_INVALID, "particleField.dat is truncated");
+  if (h->ncells != 0 && (h->ncells != ph.ncells || h->h_cell_type != ctype))
+    return fail(h, HC_ERR_INVALID, "this handle holds other cells than the checkpoint");
+  if ((rc = undo_fused_spread(h)) != HC_OK) return rc;
+  invalidate_graph(h);
+  // lattice: flags, wall velocities, body force, populations and force fields
+  lin.read((char*)h->hflag.data(), h->N);
+  if (!lin) return fail(h, HC_ERR_INVALID, "lattice.dat is truncated");
+  if ((rc = upload_flags(h)) != HC_OK) return rc;
+  std::memcpy(h->uw, lh.uw, sizeof h->uw);
+  h->body_mode = lh.body_mode;
+  for (int a = 0; a < 3; ++a) h->body[a] = lh.body[a];
+  if ((rc = upload_body(h)) != HC_OK) return rc;
+  h->cur = lh.cur;
+  h->iter = lh.iter;
+  if ((rc = get_device(h, lin, h->f[h->cur], 19 * h->ts * (size_t)h->N)) != HC_OK) return rc;
+  const size_t Fb = h->f64 ? hcd::field_bytes<double>(h->N) : hcd::field_bytes<float>(h->N);
+  for (int k = 0; k < 2; ++k)
+    if ((rc = get_device(h, lin, h->F[k], Fb)) != HC_OK) return rc;
+  // cells: a handle without cells receives them in the checkpoint's order
+  if (h->ncells == 0 && ph.ncells > 0) {
+    std::vector<double> xs((size_t)3 * ph.nvert);
+    for (int a = 0; a < 3; ++a) {
+      std::vector<double> comp(ph.nvert);
+      pin.read((char*)comp.data(), 8 * (size_t)ph.nvert);
+      for (int i = 0; i < ph.nvert; ++i) xs[3 * (size_t)i + a] = comp[i];
+    }
+    if (!pin) return fail(h, HC_ERR_INVALID, "particleField.dat is truncated");
+    int c = 0;
+    while (c < ph.ncells) {
+      int e = c;
+      while (e < ph.ncells && ctype[e] == ctype[c]) ++e;
+      const int nv = h->types[ctype[c]].tc.nv;
+      std::vector<double> part(xs.begin() + 3 * (size_t)cvoff[c], xs.begin() + 3 * ((size_t)cvoff[c] + (size_t)(e - c) * nv));
+      if ((rc = add_cells_positions(h, ctype[c], e - c, part)) != HC_OK) return rc;
+      c = e;
+    }
+    if (h->h_cell_voff != cvoff) return fail(h, HC_ERR_INVALID, "checkpoint cell layout could not be rebuilt");
+    pin.seekg((std::streamoff)(sizeof ph + 12 * (size_t)ph.ncells));
+  }
+  if (ph.nvert != h->nvert) return fail(h, HC_ERR_INVALID, "checkpoint vertex count differs");
+  if (h->ncells > 0) HC_CUDA(h, cudaMemcpyAsync(h->alive, alive.data(), 4 * (size_t)h->ncells, cudaMemcpyHostToDevice, h->stream));
+  if (h->nvert > 0) {
+    if ((rc = get_soa(h, pin, h->x, 8)) != HC_OK) return rc;
+    if ((rc = get_soa(h, pin, h->v, h->ts)) != HC_OK) return rc;
+    if ((rc = get_soa(h, pin, h->fv, h->ts)) != HC_OK) return rc;
+    if (ph.has_frep_cell) {
+      if (!(h->rep_every > 0 && h->frep_cell))
+        return fail(h, HC_ERR_INVALID, "the checkpoint holds repulsion forces: enable repulsion before loading it");
+      if ((rc = get_soa(h, pin, h->frep_cell, h->ts)) != HC_OK) return rc;
+    }
+    if (ph.has_frep_wall) {
+      if (!(h->brep_every > 0 && h->frep_wall))
+        return fail(h, HC_ERR_INVALID, "the checkpoint holds wall repulsion forces: enable it before loading");
+      if ((rc = get_soa(h, pin, h->frep_wall, h->ts)) != HC_OK) return rc;
+    }
+  }
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->spread_done = false;
   return HC_OK;
 }
 

@@ -148,6 +148,98 @@ cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f
 }
 
 // ---------------------------------------------------------------------------
+// CellInformation (helper/cellInfo.cpp:170-266), one CTA per cell: centroid,
+// mean velocity, membrane area, enclosed volume (six-term sum over faces, on
+// coordinates relative to the cell's vertex 0), largest distance between two
+// of its vertices (stretch), bounding box.  out holds 16 doubles per cell:
+// cx cy cz vx vy vz area volume stretch xmin xmax ymin ymax zmin zmax type
+// (type -1 once the cell was deleted).
+template <typename T>
+__global__ void __launch_bounds__(256) k_cell_info(const VertexView<T> vv, const int* cell_type, const int* cell_voff,
+                                                   const TypeDev* types, double* out) {
+  __shared__ double red[32][16];
+  const int cell = blockIdx.x;
+  const TypeDev& t = types[cell_type[cell]];
+  const int nv = t.nv, voff = cell_voff[cell];
+  const long long V = vv.V;
+  const double* X = vv.x;
+  const double o[3] = {X[voff], X[V + voff], X[2 * V + voff]};
+  double acc[16];
+  for (int k = 0; k < 16; ++k) acc[k] = 0.0;
+  acc[9] = acc[11] = acc[13] = 1e300;    // minima
+  acc[10] = acc[12] = acc[14] = -1e300;  // maxima
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    for (int a = 0; a < 3; ++a) {
+      const double p = X[a * V + voff + i];
+      acc[a] += p;
+      acc[3 + a] += (double)vv.v[a * V + voff + i];
+      acc[9 + 2 * a] = fmin(acc[9 + 2 * a], p);
+      acc[10 + 2 * a] = fmax(acc[10 + 2 * a], p);
+    }
+    double pi[3];
+    for (int a = 0; a < 3; ++a) pi[a] = X[a * V + voff + i];
+    for (int j = i + 1; j < nv; ++j) {
+      double d2 = 0.0;
+      for (int a = 0; a < 3; ++a) {
+        const double d = pi[a] - X[a * V + voff + j];
+        d2 += d * d;
+      }
+      acc[8] = fmax(acc[8], d2);
+    }
+  }
+  for (int k = threadIdx.x; k < t.nf; k += blockDim.x) {
+    double v[3][3];
+    for (int c = 0; c < 3; ++c)
+      for (int a = 0; a < 3; ++a) v[c][a] = X[a * V + voff + t.tris[3 * k + c]] - o[a];
+    const double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+    const double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+    const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                 cz = e1[0] * e2[1] - e1[1] * e2[0];
+    acc[6] += 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+    acc[7] += (-v[2][0] * v[1][1] * v[0][2] + v[1][0] * v[2][1] * v[0][2] + v[2][0] * v[0][1] * v[1][2] -
+               v[0][0] * v[2][1] * v[1][2] - v[1][0] * v[0][1] * v[2][2] + v[0][0] * v[1][1] * v[2][2]) /
+              6.0;
+  }
+  // block reduction: sums for 0-7, max for 8, 10, 12, 14, min for 9, 11, 13
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int k = 0; k < 15; ++k) {
+    double x = acc[k];
+    for (int off = 16; off > 0; off >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, off);
+      x = k < 8 ? x + y : ((k == 9 || k == 11 || k == 13) ? fmin(x, y) : fmax(x, y));
+    }
+    if (lane == 0) red[wid][k] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r[15];
+    for (int k = 0; k < 15; ++k) {
+      r[k] = red[0][k];
+      for (int w = 1; w < nw; ++w)
+        r[k] = k < 8 ? r[k] + red[w][k] : ((k == 9 || k == 11 || k == 13) ? fmin(r[k], red[w][k]) : fmax(r[k], red[w][k]));
+    }
+    double* dst = out + 16 * (size_t)cell;
+    for (int a = 0; a < 3; ++a) {
+      dst[a] = r[a] / nv;
+      dst[3 + a] = r[3 + a] / nv;
+    }
+    dst[6] = r[6];
+    dst[7] = r[7];
+    dst[8] = sqrt(r[8]);
+    for (int k = 9; k < 15; ++k) dst[k] = r[k];
+    dst[15] = vv.alive[cell] ? (double)cell_type[cell] : -1.0;
+  }
+}
+
+template <typename T>
+cudaError_t launch_cell_info(const VertexView<T>& vv, const int* cell_type, const int* cell_voff, const TypeDev* types,
+                             int ncells, double* out, cudaStream_t s) {
+  if (ncells <= 0) return cudaSuccess;
+  k_cell_info<T><<<ncells, 256, 0, s>>>(vv, cell_type, cell_voff, types, out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Repulsion.  k_rep_bin bins every vertex of a live cell at its node
 // int(x + 0.5) (core/hemoCellParticleField.cpp:153-156), wrapped on periodic
 // axes, and keeps its position relative to that node.  k_repulsion then
@@ -1236,6 +1328,8 @@ cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* 
 #define HC_CELL_INST(T)                                                                                        \
   template cudaError_t launch_spread<T>(const LbmView<T>&, const VertexView<T>&, double, int, cudaStream_t);   \
   template cudaError_t launch_mark_nodes<T>(const LbmView<T>&, const VertexView<T>&, cudaStream_t);            \
+  template cudaError_t launch_cell_info<T>(const VertexView<T>&, const int*, const int*, const TypeDev*, int,   \
+                                           double*, cudaStream_t);                                             \
   template cudaError_t launch_repulsion<T>(const LbmView<T>&, const VertexView<T>&, const RepView<T>&,          \
                                            cudaStream_t);                                                      \
   template cudaError_t launch_add_vertex_forces<T>(const VertexView<T>&, const int*, const double*, int,       \

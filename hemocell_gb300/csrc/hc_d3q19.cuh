@@ -150,21 +150,34 @@ __device__ __forceinline__ void pull(const LbmView<T>& L, const T* __restrict__ 
   }
 }
 
-// Mask bits of the 18 bounce-back links.
-constexpr uint32_t NB_LINKS = (1u << 18) - 1u;
-
-// True when node (X,Y,Z) with mask m can pull through the 32-bit offsets:
-// no bounce-back link and no neighbour across a face of the lattice.
+// True when node (X,Y,Z) can pull through the 32-bit offsets with its
+// bounce-back links taken inline: no neighbour across a face of the lattice
+// and one wall class among its bounce-back neighbours.
 template <typename T>
-__device__ __forceinline__ bool pull_is_interior(const LbmView<T>& L, int X, int Y, int Z, uint32_t m) {
-  return (m & NB_LINKS) == 0u && X > 0 && X < L.nx - 1 && Y > 0 && Y < L.ny - 1 && Z > 0 && Z < L.nz - 1;
+__device__ __forceinline__ bool pull_is_inline(const LbmView<T>& L, int X, int Y, int Z, uint32_t m) {
+  return (m >> NB_CLASS_SHIFT) != NB_CLASS_MIXED && X > 0 && X < L.nx - 1 && Y > 0 && Y < L.ny - 1 && Z > 0 &&
+         Z < L.nz - 1;
 }
 
-// pull() for an interior node when 19 N < 2^31: one 32-bit add per population.
+// pull() of such a node without branches: a bounce-back link reads the
+// node's own opposite population instead (one load either way) and takes
+// the moving-wall term of its class, so the lanes of a warp at a wall do not
+// diverge into the general pull.
 template <typename T>
-__device__ __forceinline__ void pull_interior(const LbmView<T>& L, const T* __restrict__ src, int n, T f[19]) {
+__device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __restrict__ src, int n, uint32_t m,
+                                            T f[19]) {
+  const int N = (int)L.N;
+  const uint32_t cls = (m >> NB_CLASS_SHIFT) & (MAX_WALL_CLASSES - 1);
+  const T ux = L.uw[cls][0], uy = L.uw[cls][1], uz = L.uw[cls][2];
+  f[0] = __ldg(src + n);
 #pragma unroll
-  for (int j = 0; j < 19; ++j) f[j] = __ldg(src + (n + L.off[j]));
+  for (int j = 1; j < 19; ++j) {
+    const int i = oppi(j);  // x - c_j == x + c_i
+    const bool bb = (m >> (i - 1)) & 1u;
+    const T v = __ldg(src + (bb ? i * N + n : n + L.off[j]));
+    const T cuw = T(cxi(i)) * ux + T(cyi(i)) * uy + T(czi(i)) * uz;
+    f[j] = bb ? v - T(6.0 * wi(i)) * cuw : v;
+  }
 }
 
 // rhoBar = sum f, j = sum c f over the shifted populations, pair-wise

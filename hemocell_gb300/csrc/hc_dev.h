@@ -43,6 +43,10 @@ struct LbmView {
   int fast;
   int off[19];
   unsigned int* status;  // device status word (bit 2: a pipeline wait timed out)
+  // the fluid nodes in lattice order, packed x | y << 10 | z << 20 (null when
+  // the lattice exceeds 1024 x 1024 x 4096 or 19 N >= 2^31)
+  const uint32_t* fluid;
+  int nfluid;
 };
 
 // status bits shared by the kernels and hc_device_status
@@ -168,6 +172,11 @@ template <typename T>
 cudaError_t launch_collide_stream_bulk(const LbmView<T>& L, const BulkPlan& P, cudaStream_t s);
 template <typename T>
 cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s);
+// the same two kernels with one thread per fluid node (L.fluid)
+template <typename T>
+cudaError_t launch_collide_stream_fluid(const LbmView<T>& L, int bs, cudaStream_t s);
+template <typename T>
+cudaError_t launch_node_velocity_fluid(const LbmView<T>& L, cudaStream_t s);
 template <typename T>
 cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s);
 template <typename T>
@@ -205,6 +214,9 @@ template <typename T>
 cudaError_t launch_soa_to_aos(const T* src, double* dst, long long V, int n, cudaStream_t s);
 template <typename T>
 cudaError_t launch_bin_vertices(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg, cudaStream_t s);
+template <typename T>
+cudaError_t launch_cell_info(const VertexView<T>& vv, const int* cell_type, const int* cell_voff, const TypeDev* types,
+                             int ncells, double* out, cudaStream_t s);
 template <typename T>
 cudaError_t launch_repulsion(const LbmView<T>& L, const VertexView<T>& vv, const RepView<T>& R, cudaStream_t s);
 // binning: tile CSR sorted by (tile, cell, vertex)

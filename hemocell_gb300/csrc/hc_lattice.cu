@@ -97,12 +97,48 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
     n = (Idx)X + (Idx)L.nx * ((Idx)Y + (Idx)L.ny * Z);
     m = __ldg(L.nbmask + n);
     if (m & NB_SOLID) return;
-    if (I32 && pull_is_interior(L, X, Y, Z, m)) pull_interior(L, L.fsrc, (int)n, f);
+    if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, m, f);
     else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   }
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
   collide_store<T, Idx>(L, n, Z, f, Fx, Fy, Fz);
+}
+
+// ---------------------------------------------------------------------------
+// K1 over the fluid nodes only.  Thread t takes the t-th fluid node in
+// lattice order (from the end when L.reverse), so no lane of a warp idles on
+// a wall node, as lanes of the (x, y)-block kernel do around a cylinder; runs
+// of consecutive fluid nodes keep the pulls coalesced.  Needs L.fluid, which
+// exists only when every index fits 32 bits.
+__device__ __forceinline__ void unpack_node(uint32_t c, int& X, int& Y, int& Z) {
+  X = (int)(c & 1023u);
+  Y = (int)((c >> 10) & 1023u);
+  Z = (int)(c >> 20);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= L.nfluid) return;
+  int X, Y, Z;
+  unpack_node(__ldg(L.fluid + (L.reverse ? L.nfluid - 1 - t : t)), X, Y, Z);
+  const int n = X + L.nx * (Y + L.ny * Z);
+  const uint32_t m = __ldg(L.nbmask + n);
+  T f[19];
+  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, m, f);
+  else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
+  T Fx, Fy, Fz;
+  FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
+  collide_store<T, int>(L, n, Z, f, Fx, Fy, Fz);
+}
+
+template <typename T>
+cudaError_t launch_collide_stream_fluid(const LbmView<T>& L, int bs, cudaStream_t s) {
+  if (L.nfluid <= 0) return cudaSuccess;
+  if (bs <= 0 || bs > 256) bs = 256;
+  k_collide_stream_fluid<T><<<(L.nfluid + bs - 1) / bs, bs, 0, s>>>(L);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -329,7 +365,7 @@ __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
   int X, Y, Z;
   node_xyz((long long)n, L.nx, L.ny, X, Y, Z);
   T f[19];
-  if (I32 && pull_is_interior(L, X, Y, Z, m)) pull_interior(L, L.fsrc, (int)n, f);
+  if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, m, f);
   else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T rhoBar, jx, jy, jz, Fx, Fy, Fz;
   moments(f, rhoBar, jx, jy, jz);
@@ -338,6 +374,33 @@ __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
   FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
                         (jz + T(0.5) * Fz) / rho);
 }
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_velocity_fluid(const LbmView<T> L) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= L.nfluid) return;
+  int X, Y, Z;
+  unpack_node(__ldg(L.fluid + (L.reverse ? L.nfluid - 1 - t : t)), X, Y, Z);
+  const int n = X + L.nx * (Y + L.ny * Z);
+  if (L.ntag[n] != *L.stamp) return;
+  const uint32_t m = L.nbmask[n];
+  T f[19];
+  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, m, f);
+  else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
+  T rhoBar, jx, jy, jz, Fx, Fy, Fz;
+  moments(f, rhoBar, jx, jy, jz);
+  FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
+  const T rho = T(1) + rhoBar;
+  FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
+                        (jz + T(0.5) * Fz) / rho);
+}
+
+template <typename T>
+cudaError_t launch_node_velocity_fluid(const LbmView<T>& L, cudaStream_t s) {
+  if (L.nfluid <= 0) return cudaSuccess;
+  k_node_velocity_fluid<T><<<(L.nfluid + 255) / 256, 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s) {
   if (L.fast) k_node_velocity<T, true><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
@@ -517,6 +580,8 @@ cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream
   template cudaError_t prepare_collide_bulk<T>(const BulkPlan&);                                           \
   template cudaError_t launch_collide_stream_bulk<T>(const LbmView<T>&, const BulkPlan&, cudaStream_t);   \
   template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                         \
+  template cudaError_t launch_node_velocity_fluid<T>(const LbmView<T>&, cudaStream_t);                   \
+  template cudaError_t launch_collide_stream_fluid<T>(const LbmView<T>&, int, cudaStream_t);             \
   template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);             \
   template cudaError_t launch_stream_out<T>(const LbmView<T>&, double*, cudaStream_t);                   \
   template cudaError_t launch_stream_in<T>(const LbmView<T>&, const double*, double, const double*,       \

@@ -346,6 +346,21 @@ class HemoCell:
         self._check(self._lib.hc_read_cells(self._h, _ip(alive), _dp(vol)))
         return alive, vol
 
+    def cell_info(self) -> np.ndarray:
+        """(cells, 16): centroid, mean velocity, area, volume, stretch, bbox, type."""
+        out = np.zeros((self.stats().cells, 16))
+        self._check(self._lib.hc_cell_info(self._h, _dp(out)))
+        return out
+
+    def writeCellInfo_CSV(self, directory: str, si_units: bool = False):
+        self._check(self._lib.hc_write_cell_info_csv(self._h, directory.encode(), 1 if si_units else 0))
+
+    def saveCheckPoint(self, directory: str):
+        self._check(self._lib.hc_save_checkpoint(self._h, directory.encode()))
+
+    def loadCheckPoint(self, directory: str):
+        self._check(self._lib.hc_load_checkpoint(self._h, directory.encode()))
+
     def read_bins(self):
         st = self.stats()
         V = st.vertices

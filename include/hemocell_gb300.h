@@ -195,6 +195,27 @@ int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_off
 int hc_bin_tiles_noalloc(const int* vertex_tile, const int* vertex_cell, int nvert, int ntiles,
                          int* tile_offsets, int* tile_vertices, int* tile_cell_offsets, int* tile_cells,
                          int max_tile_cells, void* stream);
+/* CellInformationFunctionals::calculateCellInformation (helper/cellInfo.cpp:170-266):
+ * 16 doubles per cell: centroid (inside the lattice on periodic axes), mean
+ * velocity, membrane area, volume, largest distance between two of its
+ * vertices (stretch), bounding box (xmin, xmax, ymin, ymax, zmin, zmax) and
+ * its type (-1 once deleted); lattice units */
+int hc_cell_info(hc_handle* h, double* out);
+/* writeCellInfo_CSV (io/writeCellInfoCSV.cpp:30-74): <dir>/<type name>.<iteration
+ * as 12 digits>.csv for every cell type with the reference's columns
+ * X,Y,Z,area,volume,atomic_block,cellId,baseCellId,velocity_x,velocity_y,velocity_z;
+ * si = 1 converts to SI units with dx and dt (outputInSiUnits) */
+int hc_write_cell_info_csv(hc_handle* h, const char* dir, int si);
+/* HemoCell::saveCheckPoint (core/hemoCell.cpp:210-219, core/hemoCellFields.cpp:276-319):
+ * <dir>/checkpoint.xml (iteration), <dir>/lattice.dat (flags, wall velocities,
+ * body force, post-collision populations, force fields) and
+ * <dir>/particleField.dat (cells, positions, velocities, forces, repulsion);
+ * an existing set is renamed to *.old first */
+int hc_save_checkpoint(hc_handle* h, const char* dir);
+/* HemoCell::loadCheckPoint (core/hemoCell.cpp:199-208): restores into a handle
+ * created with the same lattice size, form and cell types; a handle without
+ * cells receives the checkpoint's cells, one with cells must hold the same */
+int hc_load_checkpoint(hc_handle* h, const char* dir);
 int hc_get_stats(hc_handle* h, hc_stats* out);
 /* device status word, sticky: bit0 non-finite vertex velocity, bit1 cell
  * deleted at a wall, bit2 a shared-memory pipeline wait of the bulk-copy

@@ -65,8 +65,9 @@ def test_collide_stream_one_stage(built):
 
 
 def _k1_codes():
+    # 1: one thread per fluid node; 0x100: node velocity per fluid node;
     # bulk collide-stream: stages | CTAs per SM << 4
-    return [3 | (1 << 4), 4 | (2 << 4), 2 | (3 << 4)]
+    return [1, 0x101, 3 | (1 << 4), 4 | (2 << 4), 2 | (3 << 4)]
 
 
 @pytest.mark.parametrize("form", [0, 1])
@@ -78,16 +79,20 @@ def test_collide_stream_bulk_matches_direct(built, form, code, wall):
     case = mixed_box(wall=wall)
     a = case.build(form=form)
     b = case.build(form=form)
-    o = _orc().apply_case(case)
-    randomize(case, a, o)
-    randomize(case, b, o)
+    randomize(case, a, _orc().apply_case(case))   # one oracle each: randomize perturbs the
+    randomize(case, b, _orc().apply_case(case))   # oracle's own positions in place
     t = b.tuning()
     t[7] = code
+    if code & 0xff == 1:
+        t[0], t[1] = 256, 1
     b.set_tuning(t)
     a.stage(1)
     b.stage(1)
     assert np.array_equal(a.read_populations(), b.read_populations())
     assert np.array_equal(a.read_force_field(0), b.read_force_field(0))
+    a.stage(2)                                  # node velocity + interpolation
+    b.stage(2)
+    assert np.array_equal(a.read_vertices()[1], b.read_vertices()[1])
     assert b.device_status() == 0
     a.close()
     b.close()
