@@ -103,6 +103,7 @@ SIGNATURES = {
     "hc_bin_tiles_noalloc": (C.c_int, [P, P, C.c_int, C.c_int, P, P, P, P, C.c_int, P]),
     "hc_cell_info": (C.c_int, [P, D]),
     "hc_write_cell_info_csv": (C.c_int, [P, C.c_char_p, C.c_int]),
+    "hc_write_output": (C.c_int, [P, C.c_char_p, C.c_int]),
     "hc_save_checkpoint": (C.c_int, [P, C.c_char_p]),
     "hc_load_checkpoint": (C.c_int, [P, C.c_char_p]),
     "hc_get_stats": (C.c_int, [P, C.POINTER(hc_stats)]),
@@ -110,6 +111,7 @@ SIGNATURES = {
     "hc_autotune": (C.c_int, [P, C.c_char_p]),
     "hc_get_tuning": (C.c_int, [P, I]),
     "hc_set_tuning": (C.c_int, [P, I]),
+    "hc_stl_voxelize": (C.c_int, [C.c_char_p, C.c_int, C.c_double, C.c_int, C.c_int, I, U8, C.c_longlong]),
     "hc_mesh_icosphere": (C.c_int, [C.c_int, C.c_double, D, C.c_int, I, C.c_int, I, I]),
     "hc_mesh_rbc": (C.c_int, [C.c_int, C.c_double, D, C.c_int, I, C.c_int, I, I]),
     "hc_mesh_ellipsoid": (C.c_int, [C.c_int, C.c_double, C.c_double, D, C.c_int, I, C.c_int, I, I]),

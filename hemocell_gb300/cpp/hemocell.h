@@ -358,6 +358,10 @@ class HemoCell {
     iter = (unsigned int)st.iter;
   }
   bool outputInSiUnits = false;
+  // core/hemoCell.cpp:221-280: fluid and particle fields in <outputDirectory>/hdf5/
+  void writeOutput() {
+    check(hc_write_output(h_, outputDirectory().c_str(), outputInSiUnits ? 1 : 0));
+  }
 
   // core/hemoCell.cpp:299-376
   void iterate() {

@@ -513,6 +513,7 @@ cudaError_t launch_k1(hc_handle* h, const LbmView<T>& L) {
 
 template <typename T>
 cudaError_t launch_nv(hc_handle* h, const LbmView<T>& L) {
+  if ((h->tune[7] & 0x200) && L.fast) return hcd::launch_node_velocity_packed<T>(L, h->stream);
   if ((h->tune[7] & 0x100) && L.fluid) return hcd::launch_node_velocity_fluid<T>(L, h->stream);
   return hcd::launch_node_velocity<T>(L, h->stream);
 }
@@ -845,37 +846,6 @@ int write3(hc_handle* h, void* dst, size_t es, const double* in) {
 }
 
 // ----- autotuner: time candidate launch shapes on the live state --------
-template <typename T>
-float time_it(hc_handle* h, int reps, int which) {
-  cudaEvent_t a, b;
-  cudaEventCreate(&a);
-  cudaEventCreate(&b);
-  auto once = [&]() {
-    if (which == 0) {
-      LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
-      launch_k1<T>(h, L);
-    } else if (which == 1) {
-      LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
-      hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream);
-      launch_nv<T>(h, L);
-      hcd::launch_interp_advance<T>(L, vertex_view<T>(h), h->tg, 1, 0, h->tune[3], h->stream);
-    } else {
-      enq_mechanics<T>(h, true);
-    }
-  };
-  once();
-  cudaEventRecord(a, h->stream);
-  for (int r = 0; r < reps; ++r) once();
-  cudaEventRecord(b, h->stream);
-  cudaEventSynchronize(b);
-  float ms = 0;
-  cudaEventElapsedTime(&ms, a, b);
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  if (cudaGetLastError() != cudaSuccess) return 1e30f;
-  return ms / reps;
-}
-
 std::string tune_key(hc_handle* h) {
   std::ostringstream k;
   k << (h->f64 ? "f64" : "f32") << "_" << h->nx << "x" << h->ny << "x" << h->nz << "_V" << h->nvert << "_C"
@@ -898,87 +868,116 @@ int autotune(hc_handle* h, const char* cache) {
         return HC_OK;
       }
   }
-  // state that the candidates overwrite: the f[1-cur], F[1-cur] buffers are
-  // rewritten by the next step anyway; vertex v and force are saved.
-  const size_t vb = 3 * h->ts * (size_t)h->Vcap;
-  void *sv = nullptr, *sf = nullptr;
-  if (h->Vcap > 0) {
-    HC_CUDA(h, cudaMallocFromPoolAsync(&sv, vb, h->pool, h->stream));
-    HC_CUDA(h, cudaMallocFromPoolAsync(&sf, vb, h->pool, h->stream));
-    HC_CUDA(h, cudaMemcpyAsync(sv, h->v, vb, cudaMemcpyDeviceToDevice, h->stream));
-    HC_CUDA(h, cudaMemcpyAsync(sf, h->fv, vb, cudaMemcpyDeviceToDevice, h->stream));
+  // Every candidate runs real steps (no graph) from the same device snapshot
+  // of the state, and the fastest whole step wins; the state is put back at
+  // the end.  Timing a kernel alone on repeated inputs favours variants that
+  // reuse L2 in a way the step does not.
+  const size_t Fb = h->f64 ? hcd::field_bytes<double>(h->N) : hcd::field_bytes<float>(h->N);
+  std::vector<std::pair<void*, size_t>> parts = {{h->f[h->cur], 19 * h->ts * (size_t)h->N}, {h->F[0], Fb}, {h->F[1], Fb}};
+  if (h->Vcap > 0 && h->x) {
+    parts.push_back({h->x, 3 * 8 * (size_t)h->Vcap});
+    parts.push_back({h->v, 3 * h->ts * (size_t)h->Vcap});
+    parts.push_back({h->fv, 3 * h->ts * (size_t)h->Vcap});
   }
+  if (h->ncells > 0) parts.push_back({h->alive, 4 * (size_t)h->ncells});
+  if (h->frep_cell) parts.push_back({h->frep_cell, 3 * h->ts * (size_t)h->rep_vcap});
+  if (h->frep_wall) parts.push_back({h->frep_wall, 3 * h->ts * (size_t)h->rep_vcap});
+  parts.push_back({h->status, sizeof(unsigned int)});
+  size_t total = 0;
+  for (auto& pr : parts) total += (pr.second + 255) / 256 * 256;
+  char* snap = nullptr;
+  HC_CUDA(h, cudaMallocFromPoolAsync((void**)&snap, total, h->pool, h->stream));
+  {
+    size_t off = 0;
+    for (auto& pr : parts) {
+      HC_CUDA(h, cudaMemcpyAsync(snap + off, pr.first, pr.second, cudaMemcpyDeviceToDevice, h->stream));
+      off += (pr.second + 255) / 256 * 256;
+    }
+  }
+  const int cur0 = h->cur, iter0 = h->iter;
+  const bool sd0 = h->spread_done;
+  auto restore = [&]() -> int {
+    size_t off = 0;
+    for (auto& pr : parts) {
+      HC_CUDA(h, cudaMemcpyAsync(pr.first, snap + off, pr.second, cudaMemcpyDeviceToDevice, h->stream));
+      off += (pr.second + 255) / 256 * 256;
+    }
+    h->cur = cur0;
+    h->iter = iter0;
+    h->spread_done = sd0;
+    return HC_OK;
+  };
+  cudaEvent_t ea, eb;
+  HC_CUDA(h, cudaEventCreate(&ea));
+  HC_CUDA(h, cudaEventCreate(&eb));
+  auto trial = [&]() -> float {
+    if (restore() != HC_OK) return 1e30f;
+    for (int k = 0; k < 2; ++k)
+      if (enq_step<T>(h) != HC_OK) return 1e30f;
+    cudaEventRecord(ea, h->stream);
+    const int K = 8;
+    for (int k = 0; k < K; ++k)
+      if (enq_step<T>(h) != HC_OK) return 1e30f;
+    cudaEventRecord(eb, h->stream);
+    if (cudaEventSynchronize(eb) != cudaSuccess) return 1e30f;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ea, eb);
+    return cudaGetLastError() == cudaSuccess ? ms / K : 1e30f;
+  };
+  invalidate_graph(h);
+  // collide-stream: (x, y)-blocks, whole rows, one thread per fluid node, bulk copies
   const int k1[][2] = {{0, 1}, {0, 2}, {0, 4}, {32, 4}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {256, 1}, {32, 8}};
+  const int nvflags = h->tune[7] & 0x300;
   float best = 1e30f;
-  int bx = h->tune[0], by = h->tune[1];
+  int bx = h->tune[0], by = h->tune[1], b7 = h->tune[7] & 0xff;
+  auto try_k1 = [&](int x0, int y0, int code) {
+    h->tune[0] = x0;
+    h->tune[1] = y0;
+    h->tune[7] = code | nvflags;
+    const float t = trial();
+    if (t < best) {
+      best = t;
+      bx = x0;
+      by = y0;
+      b7 = code;
+    }
+  };
   for (auto& c : k1) {
     if (c[0] > 2 * h->nx && c[0] > 32) continue;
     if (c[0] == 0 && h->nx * c[1] > 256) continue;
-    h->tune[0] = c[0];
-    h->tune[1] = c[1];
-    float t = time_it<T>(h, 5, 0);
-    if (t < best) {
-      best = t;
-      bx = c[0];
-      by = c[1];
-    }
+    try_k1(c[0], c[1], 0);
   }
-  h->tune[0] = bx;
-  h->tune[1] = by;
-  // one thread per fluid node, and the bulk-copy variant (stages x CTAs per SM)
-  int b7 = 0;
-  h->tune[7] = 0;
   if (h->nfluid > 0)
-    for (int bs : {128, 256}) {
-      const int keep0 = h->tune[0];
-      h->tune[0] = bs;
-      h->tune[7] = 1;
-      float t = time_it<T>(h, 5, 0);
-      if (t < best) {
-        best = t;
-        b7 = 1;
-        bx = bs;
-        by = 1;
-      }
-      h->tune[0] = keep0;
-      h->tune[7] = 0;
-    }
+    for (int bs : {128, 256}) try_k1(bs, 1, 1);
   for (int ctas : {1, 2})
     for (int st : {3, 4}) {
       const int code = st | (ctas << 4);
-      if (!set_bulk_plan<T>(h, code)) continue;
-      h->tune[7] = code;
-      float t = time_it<T>(h, 5, 0);
-      if (t < best) {
-        best = t;
-        b7 = code;
-      }
-      h->tune[7] = 0;
+      if (set_bulk_plan<T>(h, code)) try_k1(bx, by, code);
     }
   h->tune[0] = bx;
   h->tune[1] = by;
-  h->tune[7] = b7;
+  h->tune[7] = b7 | nvflags;
   if (b7 >= 2) set_bulk_plan<T>(h, b7);
   if (h->nvert > 0) {
+    // node velocity variant and the IBM block size
     best = 1e30f;
-    int bb = h->tune[3];
-    const int k7 = h->tune[7] & 0xff;
-    int nvf = 0;
-    for (int fl : {0, 0x100})
+    int bb = h->tune[3], nvf = nvflags;
+    for (int fl : {0, 0x100, 0x200})
       for (int bs : {64, 128, 256}) {
-        if (fl && h->nfluid == 0) continue;
-        h->tune[3] = bs;
-        h->tune[7] = k7 | fl;
-        float t = time_it<T>(h, 5, 1);
+        if (fl == 0x100 && h->nfluid == 0) continue;
+        if (fl == 0x200 && 19LL * h->N >= (1LL << 31)) continue;
+        h->tune[2] = h->tune[3] = bs;
+        h->tune[7] = b7 | fl;
+        const float t = trial();
         if (t < best) {
           best = t;
           bb = bs;
           nvf = fl;
         }
       }
-    h->tune[3] = bb;
-    h->tune[7] = k7 | nvf;
-    h->tune[2] = bb;
+    h->tune[2] = h->tune[3] = bb;
+    h->tune[7] = b7 | nvf;
+    // membrane forces: variant x block size x grid
     best = 1e30f;
     int mb = h->tune[4], mg = h->tune[5], mv = h->tune[6];
     int sms = 0;
@@ -991,7 +990,7 @@ int autotune(hc_handle* h, const char* cache) {
           h->tune[4] = bs;
           h->tune[5] = gr;
           h->tune[6] = var;
-          float t = time_it<T>(h, 3, 2);
+          const float t = trial();
           if (t < best) {
             best = t;
             mb = bs;
@@ -1002,12 +1001,13 @@ int autotune(hc_handle* h, const char* cache) {
     h->tune[4] = mb;
     h->tune[5] = mg;
     h->tune[6] = mv;
-    HC_CUDA(h, cudaMemcpyAsync(h->v, sv, vb, cudaMemcpyDeviceToDevice, h->stream));
-    HC_CUDA(h, cudaMemcpyAsync(h->fv, sf, vb, cudaMemcpyDeviceToDevice, h->stream));
   }
+  int rc = restore();
+  cudaEventDestroy(ea);
+  cudaEventDestroy(eb);
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
-  dfree(h, sv);
-  dfree(h, sf);
+  HC_CUDA(h, cudaFreeAsync(snap, h->stream));
+  if (rc != HC_OK) return rc;
   invalidate_graph(h);
   if (cache && *cache) {
     std::ofstream out(cache, std::ios::app);
@@ -1754,7 +1754,10 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
   if (in8[6] != 0 && in8[6] != 1) return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather) or 1 (scatter)");
   {
     const int mode = in8[7] & 0xff;
-    if ((in8[7] & ~0x1ff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-8 are defined");
+    if ((in8[7] & ~0x3ff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-9 are defined");
+    if ((in8[7] & 0x300) == 0x300) return fail(h, HC_ERR_INVALID, "tune[7]: one node-velocity variant at a time");
+    if ((in8[7] & 0x200) && 19LL * h->N >= (1LL << 31))
+      return fail(h, HC_ERR_INVALID, "packed node velocity needs 19 N < 2^31");
     if ((mode == 1 || (in8[7] & 0x100)) && h->nfluid == 0)
       return fail(h, HC_ERR_INVALID, "no fluid-node list for this lattice");
     if (mode >= 2) {
@@ -1818,6 +1821,129 @@ int hc_write_cell_info_csv(hc_handle* h, const char* dir, int si) {
       out << r[0] * lp << "," << r[1] * lp << "," << r[2] * lp << "," << r[6] * la << "," << r[7] * lv << ",0,"
           << c << "," << c << "," << r[3] * lu << "," << r[4] * lu << "," << r[5] * lu << "\n";
     }
+  }
+  return HC_OK;
+}
+
+// ---- field output (content of io/FluidHdf5IO.hh and io/ParticleHdf5IO.cpp) ----
+namespace {
+
+bool write_raw(const std::string& path, const void* data, size_t bytes) {
+  std::ofstream out(path, std::ios::binary | std::ios::trunc);
+  out.write((const char*)data, (std::streamsize)bytes);
+  return (bool)out;
+}
+
+std::string xdmf_item(const std::string& file, const std::string& dims, const char* type, int precision) {
+  return "<DataItem Format=\"Binary\" Endian=\"Little\" NumberType=\"" + std::string(type) + "\" Precision=\"" +
+         std::to_string(precision) + "\" Dimensions=\"" + dims + "\">" + file + "</DataItem>";
+}
+
+}  // namespace
+
+int hc_write_output(hc_handle* h, const char* dir, int si) {
+  if (!h || !dir) return HC_ERR_INVALID;
+  std::error_code ec;
+  std::filesystem::create_directories(std::string(dir) + "/hdf5", ec);
+  if (ec) return fail(h, HC_ERR_INVALID, "cannot create " + std::string(dir) + ": " + ec.message());
+  const std::string d = std::string(dir) + "/hdf5/";
+  char it[32];
+  std::snprintf(it, sizeof it, "%012d", h->iter);
+  const double dx = h->p.dx, dt = h->p.dt;
+  const double su = si ? dx / dt : 1.0, sr = si ? h->p.rho_p : 1.0, sf = si ? h->u.df : 1.0, sl = si ? dx : 1.0;
+  int rc;
+  // fluid: Velocity, Density, Force on the nodes (x fastest)
+  {
+    const long long N = h->N;
+    std::vector<double> rho(N), u(3 * N), F(3 * N);
+    if ((rc = hc_read_fluid(h, rho.data(), u.data())) != HC_OK) return rc;
+    if ((rc = hc_read_force_field(h, F.data(), 1)) != HC_OK) return rc;
+    std::vector<float> vel(3 * N), den(N), frc(3 * N);
+    for (long long n = 0; n < N; ++n) {
+      den[n] = (float)(rho[n] * sr);
+      for (int a = 0; a < 3; ++a) {
+        vel[3 * n + a] = (float)(u[a * N + n] * su);
+        frc[3 * n + a] = (float)(F[a * N + n] * sf);
+      }
+    }
+    const std::string base = std::string("Fluid.") + it;
+    if (!write_raw(d + base + ".Velocity.bin", vel.data(), 4 * vel.size()) ||
+        !write_raw(d + base + ".Density.bin", den.data(), 4 * den.size()) ||
+        !write_raw(d + base + ".Force.bin", frc.data(), 4 * frc.size()))
+      return fail(h, HC_ERR_INVALID, "cannot write the fluid fields to " + d);
+    const std::string dims = std::to_string(h->nz) + " " + std::to_string(h->ny) + " " + std::to_string(h->nx);
+    std::ofstream x(d + base + ".xmf", std::ios::trunc);
+    x << "<?xml version=\"1.0\" ?>\n<Xdmf Version=\"2.0\">\n <Domain>\n  <Grid Name=\"Fluid\" GridType=\"Uniform\">\n"
+      << "   <Time Value=\"" << h->iter * (si ? dt : 1.0) << "\"/>\n"
+      << "   <Topology TopologyType=\"3DCoRectMesh\" Dimensions=\"" << dims << "\"/>\n"
+      << "   <Geometry GeometryType=\"ORIGIN_DXDYDZ\">\n    <DataItem Format=\"XML\" Dimensions=\"3\">0 0 0</DataItem>\n"
+      << "    <DataItem Format=\"XML\" Dimensions=\"3\">" << sl << " " << sl << " " << sl << "</DataItem>\n   </Geometry>\n"
+      << "   <Attribute Name=\"Velocity\" AttributeType=\"Vector\" Center=\"Node\">"
+      << xdmf_item(base + ".Velocity.bin", dims + " 3", "Float", 4) << "</Attribute>\n"
+      << "   <Attribute Name=\"Density\" AttributeType=\"Scalar\" Center=\"Node\">"
+      << xdmf_item(base + ".Density.bin", dims, "Float", 4) << "</Attribute>\n"
+      << "   <Attribute Name=\"Force\" AttributeType=\"Vector\" Center=\"Node\">"
+      << xdmf_item(base + ".Force.bin", dims + " 3", "Float", 4) << "</Attribute>\n"
+      << "  </Grid>\n </Domain>\n</Xdmf>\n";
+    if (!x) return fail(h, HC_ERR_INVALID, "cannot write " + d + base + ".xmf");
+  }
+  // particles per cell type: Position (geometry), Triangles (topology),
+  // Velocity, Total force (membrane + repulsion), Cell Id, of the live cells
+  const int V = h->nvert;
+  std::vector<double> x(3 * (size_t)V), v(3 * (size_t)V), f(3 * (size_t)V), rep(3 * (size_t)V, 0.0);
+  std::vector<int> alive(h->ncells);
+  if (V > 0) {
+    if ((rc = hc_read_vertices(h, x.data(), v.data(), f.data())) != HC_OK) return rc;
+    if ((h->rep_every > 0 || h->brep_every > 0) && (rc = hc_read_repulsion(h, rep.data())) != HC_OK) return rc;
+  }
+  if (h->ncells > 0) {
+    HC_CUDA(h, cudaMemcpyAsync(alive.data(), h->alive, 4 * (size_t)h->ncells, cudaMemcpyDeviceToHost, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  for (size_t ty = 0; ty < h->types.size(); ++ty) {
+    const hcg::TypeConstants& tc = h->types[ty].tc;
+    std::vector<float> pos, vel, frc;
+    std::vector<int> tri, cid;
+    int nv_out = 0;
+    for (int c = 0; c < h->ncells; ++c) {
+      if (h->h_cell_type[c] != (int)ty || !alive[c]) continue;
+      const int off = h->h_cell_voff[c];
+      for (int k = 0; k < tc.nf; ++k)
+        for (int q = 0; q < 3; ++q) tri.push_back(nv_out + tc.tris[3 * k + q]);
+      for (int k = 0; k < tc.nv; ++k) {
+        const size_t i = 3 * (size_t)(off + k);
+        for (int a = 0; a < 3; ++a) {
+          pos.push_back((float)(x[i + a] * sl));
+          vel.push_back((float)(v[i + a] * su));
+          frc.push_back((float)((f[i + a] + rep[i + a]) * sf));
+        }
+        cid.push_back(c);
+      }
+      nv_out += tc.nv;
+    }
+    const std::string base = h->types[ty].name + "." + it;
+    if (!write_raw(d + base + ".Position.bin", pos.data(), 4 * pos.size()) ||
+        !write_raw(d + base + ".Triangles.bin", tri.data(), 4 * tri.size()) ||
+        !write_raw(d + base + ".Velocity.bin", vel.data(), 4 * vel.size()) ||
+        !write_raw(d + base + ".TotalForce.bin", frc.data(), 4 * frc.size()) ||
+        !write_raw(d + base + ".CellId.bin", cid.data(), 4 * cid.size()))
+      return fail(h, HC_ERR_INVALID, "cannot write the particle fields to " + d);
+    const std::string nvs = std::to_string(nv_out), nfs = std::to_string(tri.size() / 3);
+    std::ofstream xf(d + base + ".xmf", std::ios::trunc);
+    xf << "<?xml version=\"1.0\" ?>\n<Xdmf Version=\"2.0\">\n <Domain>\n  <Grid Name=\"" << h->types[ty].name
+       << "\" GridType=\"Uniform\">\n   <Time Value=\"" << h->iter * (si ? dt : 1.0) << "\"/>\n"
+       << "   <Topology TopologyType=\"Triangle\" NumberOfElements=\"" << nfs << "\">"
+       << xdmf_item(base + ".Triangles.bin", nfs + " 3", "Int", 4) << "</Topology>\n"
+       << "   <Geometry GeometryType=\"XYZ\">" << xdmf_item(base + ".Position.bin", nvs + " 3", "Float", 4)
+       << "</Geometry>\n"
+       << "   <Attribute Name=\"Velocity\" AttributeType=\"Vector\" Center=\"Node\">"
+       << xdmf_item(base + ".Velocity.bin", nvs + " 3", "Float", 4) << "</Attribute>\n"
+       << "   <Attribute Name=\"Total force\" AttributeType=\"Vector\" Center=\"Node\">"
+       << xdmf_item(base + ".TotalForce.bin", nvs + " 3", "Float", 4) << "</Attribute>\n"
+       << "   <Attribute Name=\"Cell Id\" AttributeType=\"Scalar\" Center=\"Node\">"
+       << xdmf_item(base + ".CellId.bin", nvs, "Int", 4) << "</Attribute>\n"
+       << "  </Grid>\n </Domain>\n</Xdmf>\n";
+    if (!xf) return fail(h, HC_ERR_INVALID, "cannot write " + d + base + ".xmf");
   }
   return HC_OK;
 }
@@ -2032,6 +2158,27 @@ int hc_load_checkpoint(hc_handle* h, const char* dir) {
   }
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   h->spread_done = false;
+  return HC_OK;
+}
+
+// ---- geometry ---------------------------------------------------------------
+int hc_stl_voxelize(const char* path, int ref_dir, double ref_length, int margin, int open_ends, int* dims3,
+                    uint8_t* flags, long long max_nodes) {
+  if (!path || !dims3) return HC_ERR_INVALID;
+  std::vector<std::array<hcg::Vec3, 3>> tris;
+  std::string err = hcg::read_stl(path, tris);
+  std::vector<uint8_t> fl;
+  if (err.empty()) err = hcg::voxelize(tris, ref_dir, ref_length, margin, open_ends != 0, dims3, fl);
+  if (!err.empty()) {
+    hcd::set_handleless_error("hc_stl_voxelize: " + err);
+    return HC_ERR_INVALID;
+  }
+  if (!flags) return HC_OK;
+  if ((long long)fl.size() > max_nodes) {
+    hcd::set_handleless_error("hc_stl_voxelize: flags buffer holds fewer nodes than the lattice");
+    return HC_ERR_INVALID;
+  }
+  std::memcpy(flags, fl.data(), fl.size());
   return HC_OK;
 }
 

@@ -150,23 +150,29 @@ __device__ __forceinline__ void pull(const LbmView<T>& L, const T* __restrict__ 
   }
 }
 
-// True when node (X,Y,Z) can pull through the 32-bit offsets with its
-// bounce-back links taken inline: no neighbour across a face of the lattice
-// and one wall class among its bounce-back neighbours.
+// True when node (X,Y,Z) with mask m can take pull_inline: its bounce-back
+// neighbours share one wall class (a node bordering walls of different
+// classes keeps the general pull).
 template <typename T>
-__device__ __forceinline__ bool pull_is_inline(const LbmView<T>& L, int X, int Y, int Z, uint32_t m) {
-  return (m >> NB_CLASS_SHIFT) != NB_CLASS_MIXED && X > 0 && X < L.nx - 1 && Y > 0 && Y < L.ny - 1 && Z > 0 &&
-         Z < L.nz - 1;
+__device__ __forceinline__ bool pull_is_inline(const LbmView<T>&, int, int, int, uint32_t m) {
+  return (m >> NB_CLASS_SHIFT) != NB_CLASS_MIXED;
 }
 
-// pull() of such a node without branches: a bounce-back link reads the
-// node's own opposite population instead (one load either way) and takes
-// the moving-wall term of its class, so the lanes of a warp at a wall do not
-// diverge into the general pull.
+// pull() without branches when 19 N < 2^31.  Population j comes from
+// n + off[j], corrected by the lattice length on any axis where the
+// neighbour x - c_j wraps around (a non-periodic axis never wraps here: a
+// link leaving the lattice is a bounce-back link).  A bounce-back link reads
+// the node's own opposite population instead (one load either way) and takes
+// the moving-wall term of its class, so the lanes of a warp at a wall or on
+// a face of the lattice do not diverge into the general pull.
 template <typename T>
-__device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __restrict__ src, int n, uint32_t m,
-                                            T f[19]) {
-  const int N = (int)L.N;
+__device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __restrict__ src, int n, int X, int Y, int Z,
+                                            uint32_t m, T f[19]) {
+  const int N = (int)L.N, nx = L.nx, nxy = L.nx * L.ny;
+  // index corrections for pulling from x-1 (c_x > 0) and from x+1 (c_x < 0), per axis
+  const int cxm = X == 0 ? nx : 0, cxp = X == nx - 1 ? -nx : 0;
+  const int cym = Y == 0 ? nxy : 0, cyp = Y == L.ny - 1 ? -nxy : 0;
+  const int czm = Z == 0 ? N : 0, czp = Z == L.nz - 1 ? -N : 0;
   const uint32_t cls = (m >> NB_CLASS_SHIFT) & (MAX_WALL_CLASSES - 1);
   const T ux = L.uw[cls][0], uy = L.uw[cls][1], uz = L.uw[cls][2];
   f[0] = __ldg(src + n);
@@ -174,7 +180,9 @@ __device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __rest
   for (int j = 1; j < 19; ++j) {
     const int i = oppi(j);  // x - c_j == x + c_i
     const bool bb = (m >> (i - 1)) & 1u;
-    const T v = __ldg(src + (bb ? i * N + n : n + L.off[j]));
+    const int corr = (cxi(j) > 0 ? cxm : (cxi(j) < 0 ? cxp : 0)) + (cyi(j) > 0 ? cym : (cyi(j) < 0 ? cyp : 0)) +
+                     (czi(j) > 0 ? czm : (czi(j) < 0 ? czp : 0));
+    const T v = __ldg(src + (bb ? i * N + n : n + L.off[j] + corr));
     const T cuw = T(cxi(i)) * ux + T(cyi(i)) * uy + T(czi(i)) * uz;
     f[j] = bb ? v - T(6.0 * wi(i)) * cuw : v;
   }

@@ -177,6 +177,9 @@ template <typename T>
 cudaError_t launch_collide_stream_fluid(const LbmView<T>& L, int bs, cudaStream_t s);
 template <typename T>
 cudaError_t launch_node_velocity_fluid(const LbmView<T>& L, cudaStream_t s);
+// tagged nodes packed into whole warps (needs L.fast)
+template <typename T>
+cudaError_t launch_node_velocity_packed(const LbmView<T>& L, cudaStream_t s);
 template <typename T>
 cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s);
 template <typename T>

@@ -2,6 +2,9 @@
 #include "hc_host.h"
 
 #include <algorithm>
+#include <fstream>
+#include <sstream>
+#include <iterator>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -609,6 +612,125 @@ int pack_cells(int nx, int ny, int nz, const int* per, const uint8_t* solid, int
     placed++;
   }
   return placed;
+}
+
+// ---------------------------------------------------------------------------
+// STL geometry (helper/voxelizeDomain.cpp:74-152, getFlagMatrixFromSTL).
+
+std::string read_stl(const std::string& path, std::vector<std::array<Vec3, 3>>& tris) {
+  tris.clear();
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return "cannot open " + path;
+  std::vector<char> data((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+  // binary: 80-byte header, uint32 count, 50 bytes per triangle
+  if (data.size() >= 84) {
+    uint32_t n = 0;
+    std::memcpy(&n, data.data() + 80, 4);
+    if (data.size() == 84 + 50 * (size_t)n) {
+      for (uint32_t k = 0; k < n; ++k) {
+        const char* r = data.data() + 84 + 50 * (size_t)k + 12;  // skip the normal
+        std::array<Vec3, 3> t;
+        for (int c = 0; c < 3; ++c) {
+          float v[3];
+          std::memcpy(v, r + 12 * c, 12);
+          t[c] = {v[0], v[1], v[2]};
+        }
+        tris.push_back(t);
+      }
+      return "";
+    }
+  }
+  // ASCII: "vertex x y z" lines, three per facet
+  std::istringstream ss(std::string(data.begin(), data.end()));
+  std::string word;
+  std::vector<Vec3> verts;
+  while (ss >> word) {
+    if (word == "vertex") {
+      Vec3 v;
+      if (!(ss >> v.x >> v.y >> v.z)) return "malformed vertex in " + path;
+      verts.push_back(v);
+    }
+  }
+  if (verts.empty() || verts.size() % 3 != 0) return path + " is neither a binary nor an ASCII STL file";
+  for (size_t k = 0; k < verts.size(); k += 3) tris.push_back({verts[k], verts[k + 1], verts[k + 2]});
+  return "";
+}
+
+std::string voxelize(const std::vector<std::array<Vec3, 3>>& tris_in, int ref_dir, double ref_length, int margin,
+                     bool open_ends, int dims[3], std::vector<uint8_t>& flags) {
+  if (tris_in.empty()) return "no triangles";
+  if (ref_dir < 0 || ref_dir > 2 || !(ref_length > 0) || margin < 0) return "bad voxelisation parameters";
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (const auto& t : tris_in)
+    for (const auto& v : t) {
+      const double c[3] = {v.x, v.y, v.z};
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], c[a]);
+        hi[a] = std::max(hi[a], c[a]);
+      }
+    }
+  const double ext = hi[ref_dir] - lo[ref_dir];
+  if (!(ext > 0)) return "the mesh has no extent along the reference direction";
+  // scale: the mesh spans ref_length lattice units along ref_dir; it starts
+  // `margin` nodes into the lattice on every axis
+  const double sc = ref_length / ext;
+  for (int a = 0; a < 3; ++a) dims[a] = (int)std::ceil((hi[a] - lo[a]) * sc - 1e-9) + 1 + 2 * margin;
+  const long long N = (long long)dims[0] * dims[1] * dims[2];
+  if (N <= 0 || N > (1LL << 33)) return "voxelised lattice too large";
+  std::vector<std::array<Vec3, 3>> tris(tris_in.size());
+  for (size_t k = 0; k < tris.size(); ++k)
+    for (int c = 0; c < 3; ++c)
+      tris[k][c] = {(tris_in[k][c].x - lo[0]) * sc + margin, (tris_in[k][c].y - lo[1]) * sc + margin,
+                    (tris_in[k][c].z - lo[2]) * sc + margin};
+  // parity of crossings along +x for every (y, z) row of nodes; the row is
+  // nudged off the node lattice so that it never runs through an edge
+  const double ey = 1.234567e-6, ez = 2.345678e-6;
+  std::vector<std::vector<int>> rows((size_t)dims[1] * dims[2]);
+  for (size_t k = 0; k < tris.size(); ++k) {
+    double y0 = 1e300, y1 = -1e300, z0 = 1e300, z1 = -1e300;
+    for (const auto& v : tris[k]) {
+      y0 = std::min(y0, v.y);
+      y1 = std::max(y1, v.y);
+      z0 = std::min(z0, v.z);
+      z1 = std::max(z1, v.z);
+    }
+    for (int Z = std::max(0, (int)std::floor(z0)); Z <= std::min(dims[2] - 1, (int)std::ceil(z1)); ++Z)
+      for (int Y = std::max(0, (int)std::floor(y0)); Y <= std::min(dims[1] - 1, (int)std::ceil(y1)); ++Y)
+        rows[(size_t)Z * dims[1] + Y].push_back((int)k);
+  }
+  flags.assign(N, 1);
+  std::vector<double> xs;
+  for (int Z = 0; Z < dims[2]; ++Z)
+    for (int Y = 0; Y < dims[1]; ++Y) {
+      const double py = Y + ey, pz = Z + ez;
+      xs.clear();
+      for (int k : rows[(size_t)Z * dims[1] + Y]) {
+        const Vec3 &A = tris[k][0], &B = tris[k][1], &C = tris[k][2];
+        // barycentric coordinates of (py, pz) in the triangle's (y, z) projection
+        const double d = (B.y - A.y) * (C.z - A.z) - (C.y - A.y) * (B.z - A.z);
+        if (d == 0.0) continue;
+        const double u = ((py - A.y) * (C.z - A.z) - (C.y - A.y) * (pz - A.z)) / d;
+        const double v = ((B.y - A.y) * (pz - A.z) - (py - A.y) * (B.z - A.z)) / d;
+        if (u < 0 || v < 0 || u + v > 1) continue;
+        xs.push_back(A.x + u * (B.x - A.x) + v * (C.x - A.x));
+      }
+      std::sort(xs.begin(), xs.end());
+      for (size_t k = 0; k + 1 < xs.size(); k += 2)
+        for (int X = std::max(0, (int)std::ceil(xs[k])); X <= std::min(dims[0] - 1, (int)std::floor(xs[k + 1])); ++X)
+          flags[X + (size_t)dims[0] * (Y + (size_t)dims[1] * Z)] = 0;
+    }
+  if (open_ends && dims[0] >= 3) {
+    // the domain is closed: open both x ends by copying the slice next to them
+    auto copy_slice = [&](int dst, int src) {
+      for (int Z = 0; Z < dims[2]; ++Z)
+        for (int Y = 0; Y < dims[1]; ++Y)
+          flags[dst + (size_t)dims[0] * (Y + (size_t)dims[1] * Z)] = flags[src + (size_t)dims[0] * (Y + (size_t)dims[1] * Z)];
+    };
+    const int src0 = std::min(margin + 1, dims[0] - 1), src1 = std::max(dims[0] - 2 - margin, 0);
+    for (int X = 0; X < src0; ++X) copy_slice(X, src0);
+    for (int X = dims[0] - 1; X > src1; --X) copy_slice(X, src1);
+  }
+  return "";
 }
 
 }  // namespace hcg

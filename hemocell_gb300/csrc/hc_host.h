@@ -78,4 +78,13 @@ int pack_cells(int nx, int ny, int nz, const int* periodic, const uint8_t* solid
                const std::vector<Mesh>& shapes, const int* counts, double margin, unsigned long long seed,
                int max_attempts, double* centres, double* angles, int* types);
 
+// STL surfaces (binary or ASCII) and their voxelisation
+// (helper/voxelizeDomain.cpp:74-152): the mesh is scaled to span ref_length
+// lattice units along axis ref_dir and placed `margin` nodes in; nodes inside
+// the closed surface are fluid (0), the rest wall (1); open_ends copies the
+// slices next to both x ends onto them, opening a closed tube.
+std::string read_stl(const std::string& path, std::vector<std::array<Vec3, 3>>& tris);
+std::string voxelize(const std::vector<std::array<Vec3, 3>>& tris, int ref_dir, double ref_length, int margin,
+                     bool open_ends, int dims[3], std::vector<uint8_t>& flags);
+
 }  // namespace hcg

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
     n = (Idx)X + (Idx)L.nx * ((Idx)Y + (Idx)L.ny * Z);
     m = __ldg(L.nbmask + n);
     if (m & NB_SOLID) return;
-    if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, m, f);
+    if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, X, Y, Z, m, f);
     else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   }
   T Fx, Fy, Fz;
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L
   const int n = X + L.nx * (Y + L.ny * Z);
   const uint32_t m = __ldg(L.nbmask + n);
   T f[19];
-  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, m, f);
+  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, X, Y, Z, m, f);
   else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
   int X, Y, Z;
   node_xyz((long long)n, L.nx, L.ny, X, Y, Z);
   T f[19];
-  if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, m, f);
+  if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, X, Y, Z, m, f);
   else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T rhoBar, jx, jy, jz, Fx, Fy, Fz;
   moments(f, rhoBar, jx, jy, jz);
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(256) k_node_velocity_fluid(const LbmView<T> L)
   if (L.ntag[n] != *L.stamp) return;
   const uint32_t m = L.nbmask[n];
   T f[19];
-  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, m, f);
+  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, X, Y, Z, m, f);
   else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T rhoBar, jx, jy, jz, Fx, Fy, Fz;
   moments(f, rhoBar, jx, jy, jz);
@@ -392,6 +392,70 @@ __global__ void __launch_bounds__(256) k_node_velocity_fluid(const LbmView<T> L)
   const T rho = T(1) + rhoBar;
   FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
                         (jz + T(0.5) * Fz) / rho);
+}
+
+// Node velocity with the tagged nodes packed into whole warps.  A warp scans
+// a chunk of 256 consecutive nodes (8 per lane), gathers the tagged ones in
+// ascending order into shared memory and then pulls them 32 at a time, so
+// the pull runs with every lane busy whatever the density of tags, and the
+// scan costs one thread per 8 nodes.  Needs 19 N < 2^31 (L.fast).
+template <typename T>
+__device__ __forceinline__ void node_velocity_at(const LbmView<T>& L, int n) {
+  const int nxy = L.nx * L.ny;
+  const int Z = n / nxy, r = n - Z * nxy, Y = r / L.nx, X = r - Y * L.nx;
+  const uint32_t m = L.nbmask[n];
+  T f[19];
+  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, X, Y, Z, m, f);
+  else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
+  T rhoBar, jx, jy, jz, Fx, Fy, Fz;
+  moments(f, rhoBar, jx, jy, jz);
+  FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
+  const T rho = T(1) + rhoBar;
+  FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
+                        (jz + T(0.5) * Fz) / rho);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_node_velocity_packed(const LbmView<T> L) {
+  __shared__ int list[8][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int N = (int)L.N;
+  const int nchunks = (N + 255) / 256;
+  const int chunk = blockIdx.x * 8 + w;
+  if (chunk >= nchunks) return;
+  const int c = L.reverse ? nchunks - 1 - chunk : chunk;
+  const uint32_t stamp = *L.stamp;
+  const int base = c * 256 + lane * 8;
+  uint32_t bits = 0;
+  if (base + 8 <= N) {
+    const uint4 a = *reinterpret_cast<const uint4*>(L.ntag + base);
+    const uint4 b = *reinterpret_cast<const uint4*>(L.ntag + base + 4);
+    bits = (a.x == stamp) | (a.y == stamp) << 1 | (a.z == stamp) << 2 | (a.w == stamp) << 3 | (b.x == stamp) << 4 |
+           (b.y == stamp) << 5 | (b.z == stamp) << 6 | (b.w == stamp) << 7;
+  } else {
+    for (int k = 0; k < 8; ++k)
+      if (base + k < N && L.ntag[base + k] == stamp) bits |= 1u << k;
+  }
+  const int cnt = __popc(bits);
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  int pos = incl - cnt;
+  for (int k = 0; k < 8; ++k)
+    if ((bits >> k) & 1u) list[w][pos++] = base + k;
+  __syncwarp();
+  for (int r = lane; r < total; r += 32) node_velocity_at(L, list[w][r]);
+}
+
+template <typename T>
+cudaError_t launch_node_velocity_packed(const LbmView<T>& L, cudaStream_t s) {
+  const long long nchunks = (L.N + 255) / 256;
+  k_node_velocity_packed<T><<<(unsigned)((nchunks + 7) / 8), 256, 0, s>>>(L);
+  return cudaGetLastError();
 }
 
 template <typename T>
@@ -581,6 +645,7 @@ cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream
   template cudaError_t launch_collide_stream_bulk<T>(const LbmView<T>&, const BulkPlan&, cudaStream_t);   \
   template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                         \
   template cudaError_t launch_node_velocity_fluid<T>(const LbmView<T>&, cudaStream_t);                   \
+  template cudaError_t launch_node_velocity_packed<T>(const LbmView<T>&, cudaStream_t);                  \
   template cudaError_t launch_collide_stream_fluid<T>(const LbmView<T>&, int, cudaStream_t);             \
   template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);             \
   template cudaError_t launch_stream_out<T>(const LbmView<T>&, double*, cudaStream_t);                   \

@@ -355,6 +355,10 @@ class HemoCell:
     def writeCellInfo_CSV(self, directory: str, si_units: bool = False):
         self._check(self._lib.hc_write_cell_info_csv(self._h, directory.encode(), 1 if si_units else 0))
 
+    def writeOutput(self, directory: str, si_units: bool = False):
+        """Fluid and particle fields as XDMF over raw arrays in <directory>/hdf5/."""
+        self._check(self._lib.hc_write_output(self._h, directory.encode(), 1 if si_units else 0))
+
     def saveCheckPoint(self, directory: str):
         self._check(self._lib.hc_save_checkpoint(self._h, directory.encode()))
 
@@ -393,6 +397,22 @@ class HemoCell:
     def set_tuning(self, t):
         t = np.ascontiguousarray(t, np.int32)
         self._check(self._lib.hc_set_tuning(self._h, _ip(t)))
+
+
+def voxelize_stl(path: str, ref_dir: int = 0, ref_length: float = 100.0, margin: int = 1,
+                 open_ends: bool = True):
+    """getFlagMatrixFromSTL: (flags, dims) of a closed STL surface; flags per
+    node (x fastest) 0 fluid inside, 1 wall outside."""
+    lib = L.lib()
+    dims = np.zeros(3, np.int32)
+    if lib.hc_stl_voxelize(path.encode(), ref_dir, float(ref_length), margin, int(open_ends), _ip(dims), None, 0):
+        raise HemoCellError(lib.hc_last_error(None).decode())
+    n = int(np.prod(dims.astype(np.int64)))
+    flags = np.zeros(n, np.uint8)
+    if lib.hc_stl_voxelize(path.encode(), ref_dir, float(ref_length), margin, int(open_ends), _ip(dims),
+                           flags.ctypes.data_as(L.U8), n):
+        raise HemoCellError(lib.hc_last_error(None).decode())
+    return flags, tuple(int(d) for d in dims)
 
 
 def estimate_device_bytes(dims, form: int, nvertices: int, ncells: int, tile=(8, 8, 8)) -> int:

@@ -93,7 +93,8 @@ hc_handle* hc_create(const hc_params* p);
 int hc_destroy(hc_handle* h);
 const char* hc_last_error(const hc_handle* h); /* h may be NULL: last failure of a call
                                                   without a handle (hc_create,
-                                                  hc_bin_tiles_noalloc) */
+                                                  hc_bin_tiles_noalloc,
+                                                  hc_stl_voxelize) */
 /* Parameters::lbm_base_parameters (mechanics/constantConversion.cpp:36-59):
  * out = {tau, nu_lbm, dm, df, kBT_lbm, f_limit} */
 int hc_derived_units(const hc_handle* h, double* out6);
@@ -206,6 +207,13 @@ int hc_cell_info(hc_handle* h, double* out);
  * X,Y,Z,area,volume,atomic_block,cellId,baseCellId,velocity_x,velocity_y,velocity_z;
  * si = 1 converts to SI units with dx and dt (outputInSiUnits) */
 int hc_write_cell_info_csv(hc_handle* h, const char* dir, int si);
+/* HemoCell::writeOutput (core/hemoCell.cpp:221-280) with the content of
+ * io/FluidHdf5IO.hh and io/ParticleHdf5IO.cpp, as XDMF descriptors over raw
+ * little-endian arrays (HDF5 is not used): <dir>/hdf5/Fluid.<iteration>.xmf
+ * with Velocity, Density and Force on the nodes, and <dir>/hdf5/<type>.<iteration>.xmf
+ * per cell type with the live cells' Position, Triangles, Velocity,
+ * Total force (membrane + repulsion) and Cell Id; si = 1 writes SI units */
+int hc_write_output(hc_handle* h, const char* dir, int si);
 /* HemoCell::saveCheckPoint (core/hemoCell.cpp:210-219, core/hemoCellFields.cpp:276-319):
  * <dir>/checkpoint.xml (iteration), <dir>/lattice.dat (flags, wall velocities,
  * body force, post-collision populations, force fields) and
@@ -233,6 +241,16 @@ int hc_set_tuning(hc_handle* h, const int* in8);
 
 /* --- mesh helpers (helper/meshGeneratingFunctions.hh:31-271).  Buffers are
  * caller-owned; sizes are checked against max_nv / max_nf. */
+/* getFlagMatrixFromSTL (helper/voxelizeDomain.cpp:74-152): reads a binary or
+ * ASCII STL surface, scales it to span ref_length lattice units along axis
+ * ref_dir (0 x, 1 y, 2 z), places it `margin` nodes into the lattice and marks
+ * nodes inside the closed surface fluid (0), the rest wall (1); open_ends
+ * opens both x ends of a closed tube by copying the slices next to them.
+ * dims3 receives the lattice size; flags (x fastest, may be NULL to query
+ * the size) must hold max_nodes >= dims3[0]*dims3[1]*dims3[2] bytes.  Errors
+ * are described by hc_last_error(NULL). */
+int hc_stl_voxelize(const char* path, int ref_dir, double ref_length, int margin, int open_ends, int* dims3,
+                    uint8_t* flags, long long max_nodes);
 /* icosphere refined until nf >= min_triangles (constructSphereIcosahedron) */
 int hc_mesh_icosphere(int min_triangles, double radius, double* xyz, int max_nv, int* tris,
                       int max_nf, int* nv, int* nf);

@@ -110,3 +110,44 @@ def test_cell_info_and_csv(built, tmp_path):
             assert row[4] == pytest.approx(info[c, 7] * dx ** 3, rel=1e-12)
             assert row[8] == pytest.approx(info[c, 3] * dx / dt, rel=1e-12, abs=1e-300)
     hc.close()
+
+
+def test_write_output_fields(built, tmp_path):
+    """writeOutput: the XDMF descriptors name the reference's fields and the
+    raw arrays hold exactly what the readback calls return."""
+    import xml.etree.ElementTree as ET
+    case = _case()
+    hc = case.build()
+    hc.iterate(5)
+    out = str(tmp_path / "out")
+    hc.writeOutput(out)
+    d = os.path.join(out, "hdf5")
+    nx, ny, nz = case.dims
+    root = ET.parse(os.path.join(d, "Fluid.000000000005.xmf")).getroot()
+    names = [a.get("Name") for a in root.iter("Attribute")]
+    assert names == ["Velocity", "Density", "Force"]
+    vel = np.fromfile(os.path.join(d, "Fluid.000000000005.Velocity.bin"), np.float32).reshape(nz * ny * nx, 3)
+    rho, u = hc.read_fluid()
+    assert np.allclose(vel, u.T.astype(np.float32))
+    x, v, f = hc.read_vertices()
+    alive, _ = hc.read_cells()
+    written = 0
+    for t, spec in enumerate(case.types):
+        base = os.path.join(d, f"{spec.name}.000000000005")
+        root = ET.parse(base + ".xmf").getroot()
+        assert [a.get("Name") for a in root.iter("Attribute")] == ["Velocity", "Total force", "Cell Id"]
+        pos = np.fromfile(base + ".Position.bin", np.float32).reshape(-1, 3)
+        tri = np.fromfile(base + ".Triangles.bin", np.int32).reshape(-1, 3)
+        cid = np.fromfile(base + ".CellId.bin", np.int32)
+        nv = spec.mesh.nv
+        cells = [c for c, (tt, _) in enumerate(case.cells) if tt == t and alive[c]]   # deleted cells are left out
+        assert pos.shape[0] == nv * len(cells) and tri.shape[0] == spec.mesh.nf * len(cells)
+        assert sorted(set(cid.tolist())) == cells
+        for k, c in enumerate(cells):
+            c0 = sum(case.cells[q][1].shape[0] for q in range(c))
+            assert np.allclose(pos[k * nv:(k + 1) * nv], x[c0:c0 + nv].astype(np.float32))
+        if cells:
+            assert tri.max() == pos.shape[0] - 1
+        written += len(cells)
+    assert written == int(alive.sum()) > 0
+    hc.close()
