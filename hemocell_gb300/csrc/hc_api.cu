@@ -237,6 +237,7 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
   L.status = h->status;
+  L.pdl = (h->tune[7] & 0x400) ? 1 : 0;
   L.fluid = h->nfluid > 0 ? h->fluid : nullptr;
   L.nfluid = h->nfluid;
   L.fast = 19LL * h->N < (1LL << 31) ? 1 : 0;
@@ -587,11 +588,22 @@ int enq_repulsion(hc_handle* h, int it, bool force = false) {
 }
 
 bool fusable(hc_handle* h) {
-  if (h->p.launch != HC_LAUNCH_BATCHED || h->tune[6] != 0 || h->next > 0 || h->ncells == 0) return false;
+  if (h->p.launch != HC_LAUNCH_BATCHED || h->tune[6] == 1 || h->next > 0 || h->ncells == 0) return false;
   if (h->velocity_every != 1) return false;
   for (TypeSlot& ts : h->types)
     if (ts.every != 1) return false;
   return true;
+}
+
+// Shared memory the force assembly of one cell type takes in a variant: the
+// staged variant when its face and edge terms fit kStagedMax (two CTAs per
+// SM), else the vertex-centric path it falls back to.
+constexpr size_t kStagedMax = 110 * 1024;
+size_t mech_smem(const hc_handle* h, const TypeSlot& ts, int variant) {
+  const size_t gather = h->f64 ? hcd::mechanics_smem_bytes<double>(ts.tc.nv) : hcd::mechanics_smem_bytes<float>(ts.tc.nv);
+  if (variant != 2) return gather;
+  const size_t staged = hcd::mechanics_staged_bytes(ts.tc.model, ts.tc.nv, ts.tc.nf, ts.tc.ne, h->f64);
+  return staged <= kStagedMax ? staged : gather;
 }
 
 template <typename T>
@@ -609,12 +621,12 @@ int enq_mechanics(hc_handle* h, bool forced, bool fuse = false) {
   M.f_limit = (T)h->u.f_limit;
   if (h->p.launch == HC_LAUNCH_BATCHED && all_due && h->ncells > 0) {
     M.fuse_spread = fuse ? 1 : 0;
-    int maxnv = 0;
+    size_t smem = 0;
     for (TypeSlot& ts : h->types)
-      if (!ts.cells.empty()) maxnv = std::max(maxnv, ts.tc.nv);
+      if (!ts.cells.empty()) smem = std::max(smem, mech_smem(h, ts, h->tune[6]));
     M.cells = h->dcells_all;
     M.ncells = h->ncells;
-    M.dyn_smem = (int)hcd::mechanics_smem_bytes<T>(maxnv);
+    M.dyn_smem = (int)smem;
     HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], h->tune[5], h->tune[6], h->stream));
     return HC_OK;
   }
@@ -622,7 +634,7 @@ int enq_mechanics(hc_handle* h, bool forced, bool fuse = false) {
     if (ts.cells.empty() || !(forced || h->iter % ts.every == 0)) continue;
     M.cells = ts.dcells;
     M.ncells = (int)ts.cells.size();
-    M.dyn_smem = (int)hcd::mechanics_smem_bytes<T>(ts.tc.nv);
+    M.dyn_smem = (int)mech_smem(h, ts, h->tune[6]);
     HC_CUDA(h, hcd::launch_mechanics<T>(M, h->tune[4], 0, h->tune[6], h->stream));
   }
   return HC_OK;
@@ -958,6 +970,18 @@ int autotune(hc_handle* h, const char* cache) {
   h->tune[1] = by;
   h->tune[7] = b7 | nvflags;
   if (b7 >= 2) set_bulk_plan<T>(h, b7);
+  // programmatic dependent launch of the step's kernels (bit 10)
+  {
+    const int keep = h->tune[7];
+    h->tune[7] = keep | 0x400;
+    const float t = trial();
+    if (t < best) {
+      best = t;
+      b7 |= 0x400;
+    } else {
+      h->tune[7] = keep;
+    }
+  }
   if (h->nvert > 0) {
     // node velocity variant and the IBM block size
     best = 1e30f;
@@ -982,7 +1006,7 @@ int autotune(hc_handle* h, const char* cache) {
     int mb = h->tune[4], mg = h->tune[5], mv = h->tune[6];
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->p.device);
-    for (int var : {0, 1})
+    for (int var : {0, 1, 2})
       for (int bs : {128, 256, 384, 512, 768})
         for (int gr : {0, 2 * sms}) {
           if (bs > (h->f64 ? 384 : 768)) continue;
@@ -1269,9 +1293,8 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
   const size_t smem = (h->f64 ? hcd::mechanics_smem_bytes<double>(nv) : hcd::mechanics_smem_bytes<float>(nv));
   if (smem > 227 * 1024) return fail(h, HC_ERR_INVALID, "cell type too large for one CTA's shared memory");
   {
-    size_t need = smem;
-    for (TypeSlot& o : h->types)
-      need = std::max(need, h->f64 ? hcd::mechanics_smem_bytes<double>(o.tc.nv) : hcd::mechanics_smem_bytes<float>(o.tc.nv));
+    size_t need = std::max(smem, mech_smem(h, ts, 2));
+    for (TypeSlot& o : h->types) need = std::max(need, std::max(mech_smem(h, o, 0), mech_smem(h, o, 2)));
     HC_CUDA(h, h->f64 ? hcd::prepare_mechanics<double>((int)need) : hcd::prepare_mechanics<float>((int)need));
   }
   // one device blob: ints then doubles
@@ -1751,10 +1774,11 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
     if (in8[k] <= 0 || in8[k] > 512 || in8[k] % 32 != 0) return fail(h, HC_ERR_INVALID, "bad block size");
   if (in8[4] <= 0 || in8[4] > (h->f64 ? 384 : 768) || in8[4] % 32 != 0)
     return fail(h, HC_ERR_INVALID, "bad mechanics block size");
-  if (in8[6] != 0 && in8[6] != 1) return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather) or 1 (scatter)");
+  if (in8[6] < 0 || in8[6] > 2)
+    return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather), 1 (scatter) or 2 (staged gather)");
   {
     const int mode = in8[7] & 0xff;
-    if ((in8[7] & ~0x3ff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-9 are defined");
+    if ((in8[7] & ~0x7ff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-10 are defined");
     if ((in8[7] & 0x300) == 0x300) return fail(h, HC_ERR_INVALID, "tune[7]: one node-velocity variant at a time");
     if ((in8[7] & 0x200) && 19LL * h->N >= (1LL << 31))
       return fail(h, HC_ERR_INVALID, "packed node velocity needs 19 N < 2^31");

@@ -61,4 +61,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// Programmatic dependent launch (sm_90 and later).  A kernel launched with
+// the programmatic-serialisation attribute may start while the kernel before
+// it in the stream is still draining; it must wait (pdl_wait) before it
+// reads anything that kernel writes.  pdl_trigger marks the calling CTA's
+// share of the work as issued, so that the next kernel can be launched once
+// every CTA has triggered or exited.  Both are no-ops for a kernel launched
+// without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace hcd

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdint>
 
+#include "hc_async.cuh"
 #include "hc_d3q19.cuh"
 
 namespace hcd {
@@ -99,6 +100,7 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
 // with the step stamp so the interpolation evaluates only those nodes.
 template <typename T>
 __global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const VertexView<T> vv, const T f_limit) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= vv.nvert || !vv.alive[vv.vcell[i]]) return;
   const uint32_t stamp = *L.stamp;
@@ -137,14 +139,14 @@ __global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const Vertex
     L.ntag[K.node[j]] = stamp;
     FieldLayout<T>::add(F, L.N, K.node[j], fx * K.w[j], fy * K.w[j], fz * K.w[j]);
   }
+  pdl_trigger();
 }
 
 template <typename T>
 cudaError_t launch_spread(const LbmView<T>& L, const VertexView<T>& vv, double f_limit, int bs, cudaStream_t s) {
   if (vv.nvert <= 0) return cudaSuccess;
   if (bs <= 0) bs = 128;
-  k_spread<T><<<(vv.nvert + bs - 1) / bs, bs, 0, s>>>(L, vv, (T)f_limit);
-  return cudaGetLastError();
+  return launch_kernel(k_spread<T>, dim3((vv.nvert + bs - 1) / bs), dim3(bs), 0, s, L.pdl, L, vv, (T)f_limit);
 }
 
 // ---------------------------------------------------------------------------
@@ -253,6 +255,7 @@ cudaError_t launch_cell_info(const VertexView<T>& vv, const int* cell_type, cons
 // visited in ascending index order so the sums are deterministic.
 template <typename T>
 __global__ void k_rep_bin(const LbmView<T> L, const VertexView<T> vv, const RepView<T> R) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= vv.nvert) return;
   int q = -1;
@@ -286,6 +289,7 @@ __global__ void k_rep_bin(const LbmView<T> L, const VertexView<T> vv, const RepV
 
 template <typename T>
 __global__ void k_repulsion(const LbmView<T> L, const VertexView<T> vv, const RepView<T> R) {
+  pdl_wait();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= vv.nvert) return;
   const long long V = vv.V;
@@ -354,15 +358,16 @@ template <typename T>
 cudaError_t launch_repulsion(const LbmView<T>& L, const VertexView<T>& vv, const RepView<T>& R, cudaStream_t s) {
   if (vv.nvert <= 0) return cudaSuccess;
   const int g = (vv.nvert + 255) / 256;
-  k_rep_bin<T><<<g, 256, 0, s>>>(L, vv, R);
-  k_repulsion<T><<<g, 256, 0, s>>>(L, vv, R);
-  return cudaGetLastError();
+  cudaError_t e = launch_kernel(k_rep_bin<T>, dim3(g), dim3(256), 0, s, L.pdl, L, vv, R);
+  if (e != cudaSuccess) return e;
+  return launch_kernel(k_repulsion<T>, dim3(g), dim3(256), 0, s, L.pdl, L, vv, R);
 }
 
 // Tag the stencil nodes of every vertex (the interpolation run as a stage
 // of its own, without the spread of the same step).
 template <typename T>
 __global__ void k_mark_nodes(const LbmView<T> L, const VertexView<T> vv) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= vv.nvert || !vv.alive[vv.vcell[i]]) return;
   const uint32_t stamp = *L.stamp;
@@ -375,8 +380,7 @@ __global__ void k_mark_nodes(const LbmView<T> L, const VertexView<T> vv) {
 template <typename T>
 cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s) {
   if (vv.nvert <= 0) return cudaSuccess;
-  k_mark_nodes<T><<<(vv.nvert + 255) / 256, 256, 0, s>>>(L, vv);
-  return cudaGetLastError();
+  return launch_kernel(k_mark_nodes<T>, dim3((vv.nvert + 255) / 256), dim3(256), 0, s, L.pdl, L, vv);
 }
 
 // External vertex forces (HemoCellStretch::applyForce adds them to the
@@ -408,6 +412,7 @@ cudaError_t launch_add_vertex_forces(const VertexView<T>& vv, const int* ids, co
 template <typename T>
 __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, const VertexView<T> vv, const TileGrid tg,
                                                         const int do_interp, const int do_advance) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) *L.stamp += 1;
   if (i >= vv.nvert) return;
@@ -481,6 +486,7 @@ __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, cons
     vv.alive[cell] = 0;
     atomicOr(vv.status, 2u);
   }
+  pdl_trigger();
 }
 
 template <typename T>
@@ -488,8 +494,8 @@ cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, 
                                   int do_advance, int bs, cudaStream_t s) {
   if (bs <= 0) bs = 128;
   const int n = vv.nvert > 0 ? vv.nvert : 1;  // one thread at least: it advances the stamp
-  k_interp_advance<T><<<(n + bs - 1) / bs, bs, 0, s>>>(L, vv, tg, do_interp, do_advance);
-  return cudaGetLastError();
+  return launch_kernel(k_interp_advance<T>, dim3((n + bs - 1) / bs), dim3(bs), 0, s, L.pdl, L, vv, tg, do_interp,
+                       do_advance);
 }
 
 // ---------------------------------------------------------------------------
@@ -670,11 +676,258 @@ __device__ __forceinline__ V3t<T> plt_bending(const T* sx, const TypeDev& t, int
   return vscale(V1 + V2, fm * T(0.5));
 }
 
+// spreadParticleForce of the next step for global vertex gi with the force
+// just assembled (core/hemoCellParticleField.cpp:841-863): FORCE_LIMIT clamp
+// (the stored force stays unclamped, as after the reference's constitutive
+// model), plus the repulsion force, spread with the phi2 weights; the
+// stencil nodes are tagged for the interpolation.
+template <typename T>
+__device__ __forceinline__ void spread_vertex(const MechView<T>& M, int gi, V3t<T> f) {
+  const VertexView<T>& vv = M.vv;
+  const long long V = vv.V;
+  T mag = f.x * f.x;
+  mag += f.y * f.y;
+  mag += f.z * f.z;
+  mag = sqrt(mag);
+  if (mag > M.f_limit) f = vscale(f, M.f_limit / mag);
+  if (vv.frep_cell) f = f + V3t<T>{vv.frep_cell[gi], vv.frep_cell[V + gi], vv.frep_cell[2 * V + gi]};
+  if (vv.frep_wall) f = f + V3t<T>{vv.frep_wall[gi], vv.frep_wall[V + gi], vv.frep_wall[2 * V + gi]};
+  Kern<T> K;
+  ibm_weights(M.L, vv.x[gi], vv.x[V + gi], vv.x[2 * V + gi], K);
+  const uint32_t stamp = *M.L.stamp;
+  T* F = const_cast<T*>(M.L.Fcur);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (K.node[j] < 0) continue;
+    M.L.ntag[K.node[j]] = stamp;
+    FieldLayout<T>::add(F, M.L.N, K.node[j], f.x * K.w[j], f.y * K.w[j], f.z * K.w[j]);
+  }
+}
+
+// The vertex-centric force assembly of one cell (variant 0; the staged
+// variant falls back to it for cell types too large for its shared memory).
+// sx holds 6 nv T + nv bytes of shared memory after `red` (34 doubles).
+template <typename T>
+__device__ __forceinline__ void gather_cell(const MechView<T>& M, const TypeDev& t, int cell, double* red, T* sx) {
+  const VertexView<T>& vv = M.vv;
+  const long long V = vv.V;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  constexpr bool kF64 = sizeof(T) == 8;
+  const int nv = t.nv;
+  const int voff = M.cell_voff[cell];
+  T* sbf = sx + 3 * nv;  // own bending force per vertex
+  uint8_t* srn = reinterpret_cast<uint8_t*>(sbf + 3 * nv);  // valence per vertex
+  const bool alive = vv.alive[cell] != 0;
+  for (int k = tid; k < nv; k += bs) srn[k] = (uint8_t)t.ring_n[k];
+  // positions relative to the cell's vertex 0 (translation invariant forces;
+  // the volume sum stays well conditioned far from the origin)
+  const double r0x = vv.x[voff], r0y = vv.x[V + voff], r0z = vv.x[2 * V + voff];
+  for (int k = tid; k < nv; k += bs) {
+    sx[3 * k] = (T)(vv.x[voff + k] - r0x);
+    sx[3 * k + 1] = (T)(vv.x[V + voff + k] - r0y);
+    sx[3 * k + 2] = (T)(vv.x[2 * V + voff + k] - r0z);
+  }
+  __syncthreads();
+  if (!alive) {
+    for (int k = tid; k < nv; k += bs) {
+      vv.f[voff + k] = T(0);
+      vv.f[V + voff + k] = T(0);
+      vv.f[2 * V + voff + k] = T(0);
+    }
+    return;
+  }
+  // --- phase 1: face volume terms, own bending force (rbcHighOrderModel.cpp:62-68, :127-157)
+  double vol = 0.0;
+  for (int k = tid; k < t.nf; k += bs) {
+    const V3t<T> v0 = ld3(sx, t.tris[3 * k]), v1 = ld3(sx, t.tris[3 * k + 1]), v2 = ld3(sx, t.tris[3 * k + 2]);
+    if (kF64) {
+      const double v210 = (double)v2.x * v1.y * v0.z, v120 = (double)v1.x * v2.y * v0.z;
+      const double v201 = (double)v2.x * v0.y * v1.z, v021 = (double)v0.x * v2.y * v1.z;
+      const double v102 = (double)v1.x * v0.y * v2.z, v012 = (double)v0.x * v1.y * v2.z;
+      vol += (-v210 + v120 + v201 - v021 - v102 + v012);
+    } else {
+      // v0 . ((v1-v0) x (v2-v0)) == v0 . (v1 x v2): FP32 term, FP64 sum
+      vol += (double)vdot(v0, vcross(v1 - v0, v2 - v0));
+    }
+  }
+  if (t.model != 1) {
+    for (int i = tid; i < nv; i += bs) {
+      const int rn = t.ring_n[i];
+      const int* rg = t.ring + 6 * i;
+      const V3t<T> xi = ld3(sx, i);
+      V3t<T> sum = {T(0), T(0), T(0)};
+      for (int j = 0; j < rn; ++j) sum = sum + ld3(sx, rg[j]);
+      const V3t<T> mid = {fdiv(sum.x, (T)rn), fdiv(sum.y, (T)rn), fdiv(sum.z, (T)rn)};
+      const V3t<T> dev = mid - xi;
+      V3t<T> pn = {T(0), T(0), T(0)};
+      V3t<T> a = ld3(sx, rg[0]) - xi;
+      const V3t<T> first = a;
+      for (int j = 0; j < rn; ++j) {
+        const V3t<T> b = (j + 1 < rn) ? ld3(sx, rg[j + 1]) - xi : first;
+        T l;
+        pn = pn + normalized(vcross(a, b), l);
+        a = b;
+      }
+      T pl;
+      pn = normalized(pn, pl);
+      const T ndev = vdot(pn, dev);
+      const T dDev = fdiv(ndev - rest_value<T>(t.patch_d0, t.patch_d0f, i), (T)t.edge_mean_eq);
+      const V3t<T> bf = vscale(pn, (T)t.k_bend * (dDev + fdiv(dDev, fabs(T(kMaxBend) - dDev * dDev))));
+      sbf[3 * i] = bf.x;
+      sbf[3 * i + 1] = bf.y;
+      sbf[3 * i + 2] = bf.z;
+    }
+  }
+  block_sum<T>(vol, red);  // red[32] = sum over the block (synchronises)
+  // volume constraint in FP64 (rbcHighOrderModel.cpp:100-104), by one thread
+  if (tid == 0) {
+    const double volume = red[32] * (1.0 / 6.0);
+    const double vfr = (volume - t.volume_eq) / t.volume_eq;
+    const double vf = -t.k_volume * vfr / fabs(kMaxVol - vfr * vfr);
+    red[33] = vf;
+    red[31] = vf / t.area_mean_eq;
+  }
+  __syncthreads();
+  const T vforce = (T)red[33];
+  const T vforce_per_area = (T)red[31];
+  const T area_mean = (T)t.area_mean_eq;
+  const bool visc = (t.model != 0) || (t.eta_m != 0.0);
+  // --- phase 2: gather per vertex
+  for (int i = tid; i < nv; i += bs) {
+    const int rn = t.ring_n[i];
+    const V3t<T> xi = ld3(sx, i);
+    V3t<T> f = {T(0), T(0), T(0)};
+    V3t<T> vi = {T(0), T(0), T(0)};
+    if (visc) vi = {vv.v[voff + i], vv.v[V + voff + i], vv.v[2 * V + voff + i]};
+    int rs[6], rot[6];
+    T a0s[6], l0s[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      if (j < rn) {
+        rs[j] = t.ring[6 * i + j];
+        rot[j] = t.slot_rot[6 * i + j];
+        a0s[j] = rest_value<T>(t.slot_a0, t.slot_a0f, 6 * i + j);
+        l0s[j] = rest_value<T>(t.slot_l0, t.slot_l0f, 6 * i + j);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      if (j >= rn) break;
+      const int r = rs[j];
+      const int r1 = rs[j + 1 < rn ? j + 1 : 0];
+      // incident face (i, r, r1) in the reference's corner order: area force
+      // on this corner and the face's volume force
+      const V3t<T> xr = ld3(sx, r), xr1 = ld3(sx, r1);
+      const V3t<T> c0 = rot[j] == 0 ? xi : (rot[j] == 1 ? xr1 : xr);
+      const V3t<T> c1 = rot[j] == 0 ? xr : (rot[j] == 1 ? xi : xr1);
+      const V3t<T> c2 = rot[j] == 0 ? xr1 : (rot[j] == 1 ? xr : xi);
+      Face<T> F;
+      {
+        T nn;
+        const V3t<T> n = normalized(vcross(c1 - c0, c2 - c0), nn);
+        if (nn != T(0)) {
+          F.area = T(0.5) * nn;
+          F.n = n;
+        } else {
+          F.area = T(0);
+          F.n = {T(0), T(0), T(0)};
+        }
+        F.cen = {third(c0.x + c1.x + c2.x), third(c0.y + c1.y + c2.y), third(c0.z + c1.z + c2.z)};
+      }
+      const T a0 = a0s[j];
+      const T ar = fdiv(F.area - a0, a0);
+      const T afm = (T)t.k_area * (ar + fdiv(ar, fabs(T(kMaxArea) - ar * ar)));
+      f = f + vscale(F.cen - xi, afm);
+      if (kF64) f = f + vscale(vscale(F.n, vforce), F.area / area_mean);
+      else f = f + vscale(F.n, vforce_per_area * F.area);
+      // ring edge (i, r): link force toward r when stretched, viscosity
+      const int e = t.vedge[6 * i + j];
+      T L;
+      const V3t<T> uv = normalized(xr - xi, L);
+      const T l0 = l0s[j];
+      const T ef = fdiv(L - l0, l0);
+      f = f + vscale(uv, (T)t.k_link * (ef + fdiv(ef, fabs(T(kMaxLink) - ef * ef))));
+      if (visc) {
+        const V3t<T> vr = {vv.v[voff + r], vv.v[V + voff + r], vv.v[2 * V + voff + r]};
+        V3t<T> fv = vscale(vscale(uv, vdot(vr - vi, uv)), (T)t.eta_m);
+        const T mm = vnorm(fv);
+        if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
+        f = f + fv;
+      }
+      if (t.model != 1) {
+        // neighbour's bending reaction -bf_r / n_r
+        const T rnr = (T)srn[r];
+        f = f + V3t<T>{fdiv(-sbf[3 * r], rnr), fdiv(-sbf[3 * r + 1], rnr), fdiv(-sbf[3 * r + 2], rnr)};
+      } else {
+        // platelet dihedral terms: end point of edge e, outer point of the opposite edge
+        f = f + plt_bending(sx, t, e);
+        f = f - plt_bending(sx, t, t.vopp[6 * i + j]);
+      }
+    }
+    if (t.model != 1) f = f + ld3(sbf, i);
+    // inner links (pltSimpleModel.cpp:188-205, wbcHighOrderModel.cpp:202-223)
+    for (int q = t.vinner_off[i]; q < t.vinner_off[i + 1]; ++q) {
+      const int e = t.vinner[q];
+      const int o = t.inner[2 * e] == i ? t.inner[2 * e + 1] : t.inner[2 * e];
+      const V3t<T> ev = ld3(sx, o) - xi;
+      const T L = vnorm(ev);
+      const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};  // toward the partner
+      if (t.model == 1) {
+        const T l0 = rest_value<T>(t.inner_l0, t.inner_l0f, e);
+        f = f + vscale(uv, (T)t.k_link * T(5) * ((L - l0) / l0));
+      } else if (t.model == 2) {
+        if (L < T(2) * (T)t.radius) f = f - vscale(vscale(uv, T(1) - L / (T(2) * (T)t.radius)), (T)t.k_cyto);
+        if (L < T(2) * (T)t.core_radius)
+          f = f - vscale(vscale(uv, T(1) - L / (T(2) * (T)t.core_radius)), (T)t.k_inner_rigid);
+      }
+    }
+    vv.f[voff + i] = f.x;
+    vv.f[V + voff + i] = f.y;
+    vv.f[2 * V + voff + i] = f.z;
+    if (M.fuse_spread) spread_vertex(M, voff + i, f);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const MechView<T> M) {
+  pdl_wait();
   extern __shared__ double smem_d[];
   __shared__ TypeDev tshared;
   double* red = smem_d;  // 34 doubles
+  T* sx = reinterpret_cast<T*>(smem_d + 34);
+  for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
+    const int cell = M.cells[ci];
+    __syncthreads();  // previous cell fully written out
+    if (threadIdx.x == 0) tshared = M.types[M.cell_type[cell]];
+    __syncthreads();
+    gather_cell(M, tshared, cell, red, sx);
+  }
+  pdl_trigger();
+}
+
+// Staged variant (2): every face's area-force scalar, centroid and
+// area-weighted normal, and every edge's link force (with membrane viscosity
+// and the platelet dihedral force) are computed once into shared memory;
+// each vertex then gathers the terms of its incident faces and edges, its own
+// and its neighbours' bending, and its inner links.  Deterministic like the
+// vertex-centric variant, which computes each face and edge once per
+// incident vertex; a cell type whose terms do not fit the launch's shared
+// memory takes that variant's path.  Shared layout after `red` (34 doubles):
+// positions 3 nv, own bending 3 nv, faces 7 nf (centroid, area-force scalar,
+// area x unit normal), edges 3 ne (force on the lower-numbered end), platelet
+// dihedral 3 ne (platelets only), valence nv bytes.
+template <typename T>
+__host__ __device__ __forceinline__ size_t staged_smem_bytes(int model, int nv, int nf, int ne) {
+  const size_t words = 6 * (size_t)nv + 7 * (size_t)nf + 3 * (size_t)ne * (model == 1 ? 2 : 1);
+  return 34 * sizeof(double) + words * sizeof(T) + (size_t)nv;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics_staged(const MechView<T> M) {
+  pdl_wait();
+  extern __shared__ double smem_d[];
+  __shared__ TypeDev tshared;
+  double* red = smem_d;
   T* sx = reinterpret_cast<T*>(smem_d + 34);
   const VertexView<T>& vv = M.vv;
   const long long V = vv.V;
@@ -682,20 +935,26 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
   constexpr bool kF64 = sizeof(T) == 8;
   for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
     const int cell = M.cells[ci];
-    __syncthreads();  // previous cell fully written out
+    __syncthreads();
     if (tid == 0) tshared = M.types[M.cell_type[cell]];
     __syncthreads();
     const TypeDev& t = tshared;
-    const int nv = t.nv;
+    if (staged_smem_bytes<T>(t.model, t.nv, t.nf, t.ne) > (size_t)M.dyn_smem) {
+      gather_cell(M, t, cell, red, sx);
+      continue;
+    }
+    const int nv = t.nv, nf = t.nf, ne = t.ne;
+    const bool plt = t.model == 1;
+    T* sbf = sx + 3 * nv;
+    T* sface = sbf + 3 * nv;
+    T* sedge = sface + 7 * nf;
+    T* spltb = sedge + 3 * ne;
+    uint8_t* srn = reinterpret_cast<uint8_t*>(spltb + (plt ? 3 * ne : 0));
     const int voff = M.cell_voff[cell];
-    T* sbf = sx + 3 * nv;  // own bending force per vertex
-    uint8_t* srn = reinterpret_cast<uint8_t*>(sbf + 3 * nv);  // valence per vertex
     const bool alive = vv.alive[cell] != 0;
-    for (int k = tid; k < nv; k += bs) srn[k] = (uint8_t)t.ring_n[k];
-    // positions relative to the cell's vertex 0 (translation invariant forces;
-    // the volume sum stays well conditioned far from the origin)
     const double r0x = vv.x[voff], r0y = vv.x[V + voff], r0z = vv.x[2 * V + voff];
     for (int k = tid; k < nv; k += bs) {
+      srn[k] = (uint8_t)t.ring_n[k];
       sx[3 * k] = (T)(vv.x[voff + k] - r0x);
       sx[3 * k + 1] = (T)(vv.x[V + voff + k] - r0y);
       sx[3 * k + 2] = (T)(vv.x[2 * V + voff + k] - r0z);
@@ -709,29 +968,68 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
       }
       continue;
     }
-    // --- phase 1: face volume terms, own bending force (rbcHighOrderModel.cpp:62-68, :127-157)
+    const bool visc = (t.model != 0) || (t.eta_m != 0.0);
+    // --- phase A: faces, edges and bending, each once
     double vol = 0.0;
-    for (int k = tid; k < t.nf; k += bs) {
+    for (int k = tid; k < nf; k += bs) {
       const V3t<T> v0 = ld3(sx, t.tris[3 * k]), v1 = ld3(sx, t.tris[3 * k + 1]), v2 = ld3(sx, t.tris[3 * k + 2]);
+      const V3t<T> c = vcross(v1 - v0, v2 - v0);
       if (kF64) {
         const double v210 = (double)v2.x * v1.y * v0.z, v120 = (double)v1.x * v2.y * v0.z;
         const double v201 = (double)v2.x * v0.y * v1.z, v021 = (double)v0.x * v2.y * v1.z;
         const double v102 = (double)v1.x * v0.y * v2.z, v012 = (double)v0.x * v1.y * v2.z;
         vol += (-v210 + v120 + v201 - v021 - v102 + v012);
       } else {
-        // v0 . ((v1-v0) x (v2-v0)) == v0 . (v1 x v2): FP32 term, FP64 sum
-        vol += (double)vdot(v0, vcross(v1 - v0, v2 - v0));
+        vol += (double)vdot(v0, c);
+      }
+      T nn;
+      const V3t<T> n = normalized(c, nn);
+      const T area = nn != T(0) ? T(0.5) * nn : T(0);
+      const V3t<T> na = nn != T(0) ? vscale(n, area) : V3t<T>{T(0), T(0), T(0)};
+      const T a0 = rest_value<T>(t.tri_a0, t.tri_a0f, k);
+      const T ar = fdiv(area - a0, a0);
+      T* q = sface + 7 * k;
+      q[0] = third(v0.x + v1.x + v2.x);
+      q[1] = third(v0.y + v1.y + v2.y);
+      q[2] = third(v0.z + v1.z + v2.z);
+      q[3] = (T)t.k_area * (ar + fdiv(ar, fabs(T(kMaxArea) - ar * ar)));
+      q[4] = na.x;
+      q[5] = na.y;
+      q[6] = na.z;
+    }
+    for (int e = tid; e < ne; e += bs) {
+      const int a = t.edges[2 * e], b = t.edges[2 * e + 1];
+      T L;
+      const V3t<T> uv = normalized(ld3(sx, b) - ld3(sx, a), L);
+      const T l0 = rest_value<T>(t.edge_l0, t.edge_l0f, e);
+      const T ef = fdiv(L - l0, l0);
+      V3t<T> fe = vscale(uv, (T)t.k_link * (ef + fdiv(ef, fabs(T(kMaxLink) - ef * ef))));
+      if (visc) {
+        const V3t<T> va = {vv.v[voff + a], vv.v[V + voff + a], vv.v[2 * V + voff + a]};
+        const V3t<T> vb = {vv.v[voff + b], vv.v[V + voff + b], vv.v[2 * V + voff + b]};
+        V3t<T> fv = vscale(vscale(uv, vdot(vb - va, uv)), (T)t.eta_m);
+        const T mm = vnorm(fv);
+        if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
+        fe = fe + fv;
+      }
+      sedge[3 * e] = fe.x;
+      sedge[3 * e + 1] = fe.y;
+      sedge[3 * e + 2] = fe.z;
+      if (plt) {
+        const V3t<T> pb = plt_bending(sx, t, e);
+        spltb[3 * e] = pb.x;
+        spltb[3 * e + 1] = pb.y;
+        spltb[3 * e + 2] = pb.z;
       }
     }
-    if (t.model != 1) {
+    if (!plt) {
       for (int i = tid; i < nv; i += bs) {
-        const int rn = t.ring_n[i];
+        const int rn = srn[i];
         const int* rg = t.ring + 6 * i;
         const V3t<T> xi = ld3(sx, i);
         V3t<T> sum = {T(0), T(0), T(0)};
         for (int j = 0; j < rn; ++j) sum = sum + ld3(sx, rg[j]);
-        const V3t<T> mid = {fdiv(sum.x, (T)rn), fdiv(sum.y, (T)rn), fdiv(sum.z, (T)rn)};
-        const V3t<T> dev = mid - xi;
+        const V3t<T> dev = V3t<T>{fdiv(sum.x, (T)rn), fdiv(sum.y, (T)rn), fdiv(sum.z, (T)rn)} - xi;
         V3t<T> pn = {T(0), T(0), T(0)};
         V3t<T> a = ld3(sx, rg[0]) - xi;
         const V3t<T> first = a;
@@ -743,108 +1041,50 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
         }
         T pl;
         pn = normalized(pn, pl);
-        const T ndev = vdot(pn, dev);
-        const T dDev = fdiv(ndev - rest_value<T>(t.patch_d0, t.patch_d0f, i), (T)t.edge_mean_eq);
+        const T dDev = fdiv(vdot(pn, dev) - rest_value<T>(t.patch_d0, t.patch_d0f, i), (T)t.edge_mean_eq);
         const V3t<T> bf = vscale(pn, (T)t.k_bend * (dDev + fdiv(dDev, fabs(T(kMaxBend) - dDev * dDev))));
         sbf[3 * i] = bf.x;
         sbf[3 * i + 1] = bf.y;
         sbf[3 * i + 2] = bf.z;
       }
     }
-    block_sum<T>(vol, red);  // red[32] = sum over the block (synchronises)
-    // volume constraint in FP64 (rbcHighOrderModel.cpp:100-104), by one thread
+    block_sum<T>(vol, red);
     if (tid == 0) {
       const double volume = red[32] * (1.0 / 6.0);
       const double vfr = (volume - t.volume_eq) / t.volume_eq;
       const double vf = -t.k_volume * vfr / fabs(kMaxVol - vfr * vfr);
-      red[33] = vf;
       red[31] = vf / t.area_mean_eq;
     }
     __syncthreads();
-    const T vforce = (T)red[33];
     const T vforce_per_area = (T)red[31];
-    const T area_mean = (T)t.area_mean_eq;
-    const bool visc = (t.model != 0) || (t.eta_m != 0.0);
-    // --- phase 2: gather per vertex
+    // --- phase B: gather per vertex
     for (int i = tid; i < nv; i += bs) {
-      const int rn = t.ring_n[i];
+      const int rn = srn[i];
       const V3t<T> xi = ld3(sx, i);
       V3t<T> f = {T(0), T(0), T(0)};
-      V3t<T> vi = {T(0), T(0), T(0)};
-      if (visc) vi = {vv.v[voff + i], vv.v[V + voff + i], vv.v[2 * V + voff + i]};
-      int rs[6], rot[6];
-      T a0s[6], l0s[6];
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        if (j < rn) {
-          rs[j] = t.ring[6 * i + j];
-          rot[j] = t.slot_rot[6 * i + j];
-          a0s[j] = rest_value<T>(t.slot_a0, t.slot_a0f, 6 * i + j);
-          l0s[j] = rest_value<T>(t.slot_l0, t.slot_l0f, 6 * i + j);
-        }
-      }
 #pragma unroll
       for (int j = 0; j < 6; ++j) {
         if (j >= rn) break;
-        const int r = rs[j];
-        const int r1 = rs[j + 1 < rn ? j + 1 : 0];
-        // incident face (i, r, r1) in the reference's corner order: area force
-        // on this corner and the face's volume force
-        const V3t<T> xr = ld3(sx, r), xr1 = ld3(sx, r1);
-        const V3t<T> c0 = rot[j] == 0 ? xi : (rot[j] == 1 ? xr1 : xr);
-        const V3t<T> c1 = rot[j] == 0 ? xr : (rot[j] == 1 ? xi : xr1);
-        const V3t<T> c2 = rot[j] == 0 ? xr1 : (rot[j] == 1 ? xr : xi);
-        Face<T> F;
-        {
-          T nn;
-          const V3t<T> n = normalized(vcross(c1 - c0, c2 - c0), nn);
-          if (nn != T(0)) {
-            F.area = T(0.5) * nn;
-            F.n = n;
-          } else {
-            F.area = T(0);
-            F.n = {T(0), T(0), T(0)};
-          }
-          F.cen = {third(c0.x + c1.x + c2.x), third(c0.y + c1.y + c2.y), third(c0.z + c1.z + c2.z)};
-        }
-        const T a0 = a0s[j];
-        const T ar = fdiv(F.area - a0, a0);
-        const T afm = (T)t.k_area * (ar + fdiv(ar, fabs(T(kMaxArea) - ar * ar)));
-        f = f + vscale(F.cen - xi, afm);
-        if (kF64) f = f + vscale(vscale(F.n, vforce), F.area / area_mean);
-        else f = f + vscale(F.n, vforce_per_area * F.area);
-        // ring edge (i, r): link force toward r when stretched, viscosity
+        const int r = t.ring[6 * i + j];
+        const T* q = sface + 7 * t.vface[6 * i + j];
+        f = f + vscale(V3t<T>{q[0], q[1], q[2]} - xi, q[3]) + vscale(V3t<T>{q[4], q[5], q[6]}, vforce_per_area);
         const int e = t.vedge[6 * i + j];
-        T L;
-        const V3t<T> uv = normalized(xr - xi, L);
-        const T l0 = l0s[j];
-        const T ef = fdiv(L - l0, l0);
-        f = f + vscale(uv, (T)t.k_link * (ef + fdiv(ef, fabs(T(kMaxLink) - ef * ef))));
-        if (visc) {
-          const V3t<T> vr = {vv.v[voff + r], vv.v[V + voff + r], vv.v[2 * V + voff + r]};
-          V3t<T> fv = vscale(vscale(uv, vdot(vr - vi, uv)), (T)t.eta_m);
-          const T mm = vnorm(fv);
-          if (mm > T(kForceLimit / 4.0)) fv = vscale(fv, T(kForceLimit / 4.0) / mm);
-          f = f + fv;
-        }
-        if (t.model != 1) {
-          // neighbour's bending reaction -bf_r / n_r
+        const V3t<T> fe = ld3(sedge, e);
+        f = i < r ? f + fe : f - fe;
+        if (!plt) {
           const T rnr = (T)srn[r];
-          f = f + V3t<T>{fdiv(-sbf[3 * r], rnr), fdiv(-sbf[3 * r + 1], rnr), fdiv(-sbf[3 * r + 2], rnr)};
+          f = f - V3t<T>{fdiv(sbf[3 * r], rnr), fdiv(sbf[3 * r + 1], rnr), fdiv(sbf[3 * r + 2], rnr)};
         } else {
-          // platelet dihedral terms: end point of edge e, outer point of the opposite edge
-          f = f + plt_bending(sx, t, e);
-          f = f - plt_bending(sx, t, t.vopp[6 * i + j]);
+          f = f + ld3(spltb, e) - ld3(spltb, t.vopp[6 * i + j]);
         }
       }
-      if (t.model != 1) f = f + ld3(sbf, i);
-      // inner links (pltSimpleModel.cpp:188-205, wbcHighOrderModel.cpp:202-223)
+      if (!plt) f = f + ld3(sbf, i);
       for (int q = t.vinner_off[i]; q < t.vinner_off[i + 1]; ++q) {
         const int e = t.vinner[q];
         const int o = t.inner[2 * e] == i ? t.inner[2 * e + 1] : t.inner[2 * e];
         const V3t<T> ev = ld3(sx, o) - xi;
         const T L = vnorm(ev);
-        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};  // toward the partner
+        const V3t<T> uv = {ev.x / L, ev.y / L, ev.z / L};
         if (t.model == 1) {
           const T l0 = rest_value<T>(t.inner_l0, t.inner_l0f, e);
           f = f + vscale(uv, (T)t.k_link * T(5) * ((L - l0) / l0));
@@ -857,30 +1097,10 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
       vv.f[voff + i] = f.x;
       vv.f[V + voff + i] = f.y;
       vv.f[2 * V + voff + i] = f.z;
-      if (M.fuse_spread) {
-        // spreadParticleForce of the next step (core/hemoCellParticleField.cpp:841-863);
-        // the stored force stays unclamped as after the reference's constitutive model
-        T mag = f.x * f.x;
-        mag += f.y * f.y;
-        mag += f.z * f.z;
-        mag = sqrt(mag);
-        if (mag > M.f_limit) f = vscale(f, M.f_limit / mag);
-        const int gi = voff + i;
-        if (vv.frep_cell) f = f + V3t<T>{vv.frep_cell[gi], vv.frep_cell[V + gi], vv.frep_cell[2 * V + gi]};
-        if (vv.frep_wall) f = f + V3t<T>{vv.frep_wall[gi], vv.frep_wall[V + gi], vv.frep_wall[2 * V + gi]};
-        Kern<T> K;
-        ibm_weights(M.L, vv.x[voff + i], vv.x[V + voff + i], vv.x[2 * V + voff + i], K);
-        const uint32_t stamp = *M.L.stamp;
-        T* F = const_cast<T*>(M.L.Fcur);
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          if (K.node[j] < 0) continue;
-          M.L.ntag[K.node[j]] = stamp;
-          FieldLayout<T>::add(F, M.L.N, K.node[j], f.x * K.w[j], f.y * K.w[j], f.z * K.w[j]);
-        }
-      }
+      if (M.fuse_spread) spread_vertex(M, voff + i, f);
     }
   }
+  pdl_trigger();
 }
 
 // Scatter variant (selected by the tuner): one CTA per cell.  Pass A runs the faces
@@ -891,6 +1111,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
 // memory and are written once.
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics_scatter(const MechView<T> M) {
+  pdl_wait();
   extern __shared__ double smem_d[];
   __shared__ TypeDev tshared;
   double* red = smem_d;  // 34 doubles
@@ -1091,7 +1312,13 @@ template <typename T>
 cudaError_t prepare_mechanics(int smem_bytes) {
   cudaError_t e = cudaFuncSetAttribute(k_mechanics<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_mechanics_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  e = cudaFuncSetAttribute(k_mechanics_scatter<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_mechanics_staged<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+}
+
+size_t mechanics_staged_bytes(int model, int nv, int nf, int ne, bool f64) {
+  return f64 ? staged_smem_bytes<double>(model, nv, nf, ne) : staged_smem_bytes<float>(model, nv, nf, ne);
 }
 
 // variant 0: vertex-centric gather (deterministic), 1: face/edge scatter with
@@ -1102,9 +1329,9 @@ cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, int variant
   if (bs <= 0) bs = 256;
   if (bs > (sizeof(T) == 8 ? 384 : 768)) bs = sizeof(T) == 8 ? 384 : 768;
   if (grid <= 0 || grid > M.ncells) grid = M.ncells;
-  if (variant == 1) k_mechanics_scatter<T><<<grid, bs, M.dyn_smem, s>>>(M);
-  else k_mechanics<T><<<grid, bs, M.dyn_smem, s>>>(M);
-  return cudaGetLastError();
+  if (variant == 1) return launch_kernel(k_mechanics_scatter<T>, dim3(grid), dim3(bs), M.dyn_smem, s, M.L.pdl, M);
+  if (variant == 2) return launch_kernel(k_mechanics_staged<T>, dim3(grid), dim3(bs), M.dyn_smem, s, M.L.pdl, M);
+  return launch_kernel(k_mechanics<T>, dim3(grid), dim3(bs), M.dyn_smem, s, M.L.pdl, M);
 }
 
 // device [3][Vcap] (T) -> [V][3] double

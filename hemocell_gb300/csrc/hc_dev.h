@@ -47,6 +47,7 @@ struct LbmView {
   // the lattice exceeds 1024 x 1024 x 4096 or 19 N >= 2^31)
   const uint32_t* fluid;
   int nfluid;
+  int pdl;  // launch the step's kernels with programmatic dependent launch
 };
 
 // status bits shared by the kernels and hc_device_status
@@ -156,6 +157,24 @@ struct MechView {
   T f_limit;
 };
 
+// Kernel launch with or without programmatic dependent launch (the kernel
+// then starts with pdl_wait, see hc_async.cuh).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_kernel(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                          Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr.val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Launch wrappers; each enqueues on `s` and returns the launch error code.
 // hc_lattice.cu
 template <typename T>
@@ -207,6 +226,8 @@ cudaError_t launch_add_vertex_forces(const VertexView<T>& vv, const int* ids, co
 template <typename T>
 cudaError_t launch_interp_advance(const LbmView<T>& L, const VertexView<T>& vv, const TileGrid& tg,
                                   int do_interp, int do_advance, int bs, cudaStream_t s);
+// shared memory the staged force assembly (variant 2) needs for one cell type
+size_t mechanics_staged_bytes(int model, int nv, int nf, int ne, bool f64);
 template <typename T>
 cudaError_t launch_mechanics(const MechView<T>& M, int bs, int grid, int variant, cudaStream_t s);
 template <typename T>

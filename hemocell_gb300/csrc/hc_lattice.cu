@@ -72,6 +72,7 @@ __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z,
 // on the planes the previous pass wrote last, which are still in L2.
 template <typename T, bool ROWS, bool I32>
 __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
+  pdl_wait();
   // I32: every population index fits 32 bits (19 N < 2^31), so interior
   // nodes pull through L.off and all index arithmetic stays 32-bit
   using Idx = typename std::conditional<I32, int, long long>::type;
@@ -103,6 +104,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
   collide_store<T, Idx>(L, n, Z, f, Fx, Fy, Fz);
+  pdl_trigger();
 }
 
 // ---------------------------------------------------------------------------
@@ -119,6 +121,7 @@ __device__ __forceinline__ void unpack_node(uint32_t c, int& X, int& Y, int& Z) 
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L) {
+  pdl_wait();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= L.nfluid) return;
   int X, Y, Z;
@@ -131,14 +134,14 @@ __global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
   collide_store<T, int>(L, n, Z, f, Fx, Fy, Fz);
+  pdl_trigger();
 }
 
 template <typename T>
 cudaError_t launch_collide_stream_fluid(const LbmView<T>& L, int bs, cudaStream_t s) {
   if (L.nfluid <= 0) return cudaSuccess;
   if (bs <= 0 || bs > 256) bs = 256;
-  k_collide_stream_fluid<T><<<(L.nfluid + bs - 1) / bs, bs, 0, s>>>(L);
-  return cudaGetLastError();
+  return launch_kernel(k_collide_stream_fluid<T>, dim3((L.nfluid + bs - 1) / bs), dim3(bs), 0, s, L.pdl, L);
 }
 
 // ---------------------------------------------------------------------------
@@ -344,9 +347,8 @@ cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStrea
   if (bx <= 0) bx = 64;
   dim3 block(bx, by, 1);
   dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
-  if (L.fast) k_collide_stream<T, false, true><<<grid, block, 0, s>>>(L);
-  else k_collide_stream<T, false, false><<<grid, block, 0, s>>>(L);
-  return cudaGetLastError();
+  if (L.fast) return launch_kernel(k_collide_stream<T, false, true>, grid, block, 0, s, L.pdl, L);
+  return launch_kernel(k_collide_stream<T, false, false>, grid, block, 0, s, L.pdl, L);
 }
 
 // ---------------------------------------------------------------------------
@@ -356,6 +358,7 @@ cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStrea
 // L.Fcur the force of that collision.
 template <typename T, bool I32>
 __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
+  pdl_wait();
   using Idx = typename std::conditional<I32, int, long long>::type;
   const Idx g = (Idx)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= (Idx)L.N) return;
@@ -373,9 +376,11 @@ __global__ void __launch_bounds__(256) k_node_velocity(const LbmView<T> L) {
   const T rho = T(1) + rhoBar;
   FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
                         (jz + T(0.5) * Fz) / rho);
+  pdl_trigger();
 }
 template <typename T>
 __global__ void __launch_bounds__(256) k_node_velocity_fluid(const LbmView<T> L) {
+  pdl_wait();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= L.nfluid) return;
   int X, Y, Z;
@@ -392,6 +397,7 @@ __global__ void __launch_bounds__(256) k_node_velocity_fluid(const LbmView<T> L)
   const T rho = T(1) + rhoBar;
   FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
                         (jz + T(0.5) * Fz) / rho);
+  pdl_trigger();
 }
 
 // Node velocity with the tagged nodes packed into whole warps.  A warp scans
@@ -417,6 +423,7 @@ __device__ __forceinline__ void node_velocity_at(const LbmView<T>& L, int n) {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_node_velocity_packed(const LbmView<T> L) {
+  pdl_wait();
   __shared__ int list[8][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int N = (int)L.N;
@@ -449,27 +456,26 @@ __global__ void __launch_bounds__(256) k_node_velocity_packed(const LbmView<T> L
     if ((bits >> k) & 1u) list[w][pos++] = base + k;
   __syncwarp();
   for (int r = lane; r < total; r += 32) node_velocity_at(L, list[w][r]);
+  pdl_trigger();
 }
 
 template <typename T>
 cudaError_t launch_node_velocity_packed(const LbmView<T>& L, cudaStream_t s) {
   const long long nchunks = (L.N + 255) / 256;
-  k_node_velocity_packed<T><<<(unsigned)((nchunks + 7) / 8), 256, 0, s>>>(L);
-  return cudaGetLastError();
+  return launch_kernel(k_node_velocity_packed<T>, dim3((unsigned)((nchunks + 7) / 8)), dim3(256), 0, s, L.pdl, L);
 }
 
 template <typename T>
 cudaError_t launch_node_velocity_fluid(const LbmView<T>& L, cudaStream_t s) {
   if (L.nfluid <= 0) return cudaSuccess;
-  k_node_velocity_fluid<T><<<(L.nfluid + 255) / 256, 256, 0, s>>>(L);
-  return cudaGetLastError();
+  return launch_kernel(k_node_velocity_fluid<T>, dim3((L.nfluid + 255) / 256), dim3(256), 0, s, L.pdl, L);
 }
 
 template <typename T>
 cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s) {
-  if (L.fast) k_node_velocity<T, true><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
-  else k_node_velocity<T, false><<<(unsigned)((L.N + 255) / 256), 256, 0, s>>>(L);
-  return cudaGetLastError();
+  const dim3 g((unsigned)((L.N + 255) / 256));
+  if (L.fast) return launch_kernel(k_node_velocity<T, true>, g, dim3(256), 0, s, L.pdl, L);
+  return launch_kernel(k_node_velocity<T, false>, g, dim3(256), 0, s, L.pdl, L);
 }
 
 // Fluid readback: rho and u of every node (post-stream, force of the last collision).

@@ -235,8 +235,12 @@ int hc_autotune(hc_handle* h, const char* cache_path);
 int hc_get_tuning(hc_handle* h, int* out8);
 /* in8: collide-stream block (bx, by; bx = 0 whole rows), spread block,
  * interpolation block, mechanics block, mechanics grid (0 = one CTA per cell),
- * mechanics variant (0 vertex gather, 1 face/edge scatter), bulk-copy
- * collide-stream (0 off, else stages | CTAs per SM << 4) */
+ * mechanics variant (0 vertex gather, 1 face/edge scatter, 2 staged face/edge
+ * terms gathered per vertex), and in8[7]: bits 0-7 the collide-stream kind
+ * (0 (x,y)-blocks or rows, 1 one thread per fluid node, else bulk copies:
+ * stages | CTAs per SM << 4), bit 8 node velocity per fluid node, bit 9 node
+ * velocity over warp-packed tagged nodes, bit 10 programmatic dependent launch
+ * of the step's kernels */
 int hc_set_tuning(hc_handle* h, const int* in8);
 
 /* --- mesh helpers (helper/meshGeneratingFunctions.hh:31-271).  Buffers are

@@ -262,11 +262,12 @@ def test_advance_and_bins_bit_exact(built):
     hc.close()
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("types", [[0], [1], [2], [0, 1, 2]])
 def test_mechanics_stage(built, types, variant):
-    """Both force-assembly variants (0 vertex gather, 1 face/edge scatter)
-    against the oracle's face/edge/vertex loops."""
+    """The three force-assembly variants (0 vertex gather, 1 face/edge
+    scatter, 2 staged face/edge terms gathered per vertex) against the
+    oracle's face/edge/vertex loops."""
     case = mixed_box()
     case.cells = [c for c in case.cells if c[0] in types]
     hc = case.build()
@@ -281,11 +282,53 @@ def test_mechanics_stage(built, types, variant):
     _, _, fo = o.read_vertices()
     assert np.abs(fo).max() > 0
     assert rel_l2(fg, fo) < STAGE_TOL
-    if variant == 0:  # no atomics: the same inputs give the same bits
+    if variant != 1:  # no atomics: the same inputs give the same bits
         hc.stage(5)
         _, _, fg2 = hc.read_vertices()
         assert np.array_equal(fg, fg2)
     hc.close()
+
+
+@pytest.mark.parametrize("variant", [0, 2])
+def test_mechanics_stage_fp32(built, variant):
+    """FP32 force assembly against the FP64 oracle (all three cell types)."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box()
+    hc = case.build(form=L.HC_FORM_MIXED_F32)
+    t = hc.tuning()
+    t[6] = variant
+    hc.set_tuning(t)
+    o = _orc().apply_case(case)
+    randomize(case, hc, o, xamp=0.08)
+    hc.stage(5)
+    o.stage("mechanics", forced=1)
+    assert rel_l2(hc.read_vertices()[2], o.read_vertices()[2]) < 2e-5
+    hc.close()
+
+
+def test_staged_mechanics_falls_back_for_large_cells(built):
+    """A 2562-vertex WBC does not fit the staged variant's shared memory in
+    FP32: that cell takes the vertex-centric path (compiled into the other
+    kernel, so only FP32 rounding may differ)."""
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    t = C.wbc_type(5120)
+    n = (40, 40, 40)
+    xyz = C.place_cells(t.mesh, np.array([[19.5, 19.5, 19.5]]), np.array([[0.3, 0.2, 0.1]]))
+    case = C.Case("wbc", n, (1, 1, 1), types=[t], cells=[(0, xyz)])
+    out = []
+    for variant in (0, 2):
+        hc = case.build(form=L.HC_FORM_MIXED_F32)
+        tt = hc.tuning()
+        tt[6] = variant
+        hc.set_tuning(tt)
+        rng = np.random.default_rng(4)
+        x, _, _ = hc.read_vertices()
+        hc.write_vertices(x + 0.05 * rng.standard_normal(x.shape), None, None)
+        hc.stage(5)
+        out.append(hc.read_vertices()[2])
+        hc.close()
+    assert np.abs(out[0]).max() > 0 and rel_l2(out[1], out[0]) < 1e-6
 
 
 def mixed_periodic(seed=9):
@@ -449,3 +492,24 @@ def test_error_paths(built):
     with pytest.raises(HemoCellError):
         hc.stage(42)
     hc.close()
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_programmatic_dependent_launch_same_results(built, form):
+    """The step's kernels launched with programmatic dependent launch (tune[7]
+    bit 10) give the results of ordinary launches, batched and graph-replayed."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=True)
+    a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    t = b.tuning()
+    t[7] |= 0x400
+    b.set_tuning(t)
+    a.iterate(40)
+    b.iterate(40)
+    tol = RUN_TOL if form == 0 else 1e-5
+    assert rel_l2(b.read_vertices()[0], a.read_vertices()[0]) < tol
+    assert rel_l2(b.read_fluid()[1], a.read_fluid()[1]) < tol
+    assert b.device_status() == a.device_status()
+    a.close()
+    b.close()
