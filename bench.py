@@ -48,6 +48,18 @@ BYTES_VERTEX = {"f32": 2 * 3 * 8 + 2 * 2 * 3 * 4, "f64": 2 * 3 * 3 * 8}
 K1_TRAFFIC_PER_LAUNCH = {"f32": 105.014784e6 + 33.601536e6, "f64": 174.845696e6 + 93.809152e6}
 
 
+def cpu_model() -> str:
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith(("model name", "cpu part", "hardware")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -238,6 +250,7 @@ def kolmogorov_leg(steps: int, warmup: int, tune_cache):
         out[name] = {"value": case.N * steps / (ms * 1e3), "unit": "MLUPS", "ms_per_step": ms / steps,
                      "stages_ms": prof, "tuning": tuning, "status": status, "clocks": clocks}
     out["fp32_over_fp64"] = out["fp32_batched"]["value"] / out["fp64_batched"]["value"]
+    out["_case"] = case
     return out
 
 
@@ -389,7 +402,18 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu_val, n_cpu, cores = cpu_baseline(case)
         cpu = {"value": cpu_val, "unit": "MLUPS", "cores": cores, "kind": "port",
-               "sample": f"{n_cpu} full steps of the same workload (FP64 CPU restatement, OpenMP)"}
+               "sample": f"{n_cpu} full steps of the same workload (FP64 CPU restatement, OpenMP)",
+               "label": "CPU restatement of HemoCell (not the HemoCell binary)", "cpu": cpu_model()}
+        # the other configurations, bounded slices
+        from hemocell_gb300 import cases
+        shear = cases.shear_single_rbc(n=50, shear_rate=100.0, seed=1)
+        v0, n0, _ = cpu_baseline(shear, budget_s=4.0)
+        cpu["shear_rbc_50"] = {"value": v0, "unit": "MLUPS", "sample": f"{n0} steps of the 50^3 sheared RBC"}
+        if "kolmogorov" in extra and "_case" in extra["kolmogorov"]:
+            v3, n3, _ = cpu_baseline(extra["kolmogorov"]["_case"], budget_s=8.0)
+            cpu["kolmogorov_128"] = {"value": v3, "unit": "MLUPS", "sample": f"{n3} steps of the 128^3 suspension"}
+    if "kolmogorov" in extra:
+        extra["kolmogorov"].pop("_case", None)
 
     if rank == 0:
         line = {
