@@ -127,6 +127,10 @@ struct hc_handle {
   // pass (fused spread); anything that changes forces, positions or the
   // force field between steps clears it
   bool spread_done = false;
+  // the last force assembly interpolated and advanced the vertices itself and
+  // tagged the stencil nodes with stamp + 1: the next collide-stream (or a
+  // state change) advances the stamp
+  bool stamp_ahead = false;
   // external vertex forces (HemoCellStretch)
   int next = 0, next_cap = 0;
   int* ext_ids = nullptr;
@@ -238,6 +242,7 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
     for (int a = 0; a < 3; ++a) L.uw[c][a] = (T)h->uw[c][a];
   L.status = h->status;
   L.pdl = (h->tune[7] & 0x400) ? 1 : 0;
+  L.bump_stamp = 0;
   L.fluid = h->nfluid > 0 ? h->fluid : nullptr;
   L.nfluid = h->nfluid;
   L.fast = 19LL * h->N < (1LL << 31) ? 1 : 0;
@@ -481,6 +486,11 @@ int upload_cell_lists(hc_handle* h) {
 // spread.  A change that makes that spread stale restores the field to the
 // body force so the next step spreads afresh.
 int undo_fused_spread(hc_handle* h) {
+  if (h->stamp_ahead) {
+    // catch the stamp up with the tags the fused spread wrote
+    HC_CUDA(h, hcd::launch_bump_stamp(h->stamp, h->stream));
+    h->stamp_ahead = false;
+  }
   if (!h->spread_done) return HC_OK;
   const long long plane = (long long)h->nx * h->ny;
   if (h->f64)
@@ -522,6 +532,8 @@ cudaError_t launch_nv(hc_handle* h, const LbmView<T>& L) {
 template <typename T>
 int enq_collide(hc_handle* h) {
   LbmView<T> L = lbm_view<T>(h, h->cur, h->cur);
+  L.bump_stamp = h->stamp_ahead ? 1 : 0;
+  h->stamp_ahead = false;
   HC_CUDA(h, launch_k1<T>(h, L));
   h->cur ^= 1;
   return HC_OK;
@@ -607,7 +619,7 @@ size_t mech_smem(const hc_handle* h, const TypeSlot& ts, int variant) {
 }
 
 template <typename T>
-int enq_mechanics(hc_handle* h, bool forced, bool fuse = false) {
+int enq_mechanics(hc_handle* h, bool forced, bool fuse = false, bool fuse_adv = false) {
   bool all_due = true;
   for (TypeSlot& ts : h->types)
     if (!(forced || h->iter % ts.every == 0)) all_due = false;
@@ -617,10 +629,15 @@ int enq_mechanics(hc_handle* h, bool forced, bool fuse = false) {
   M.types = h->dtypes;
   M.vv = vertex_view<T>(h);
   M.fuse_spread = 0;
-  M.L = lbm_view<T>(h, h->cur, h->cur);  // Fcur = the next step's force field
+  M.fuse_advance = 0;
+  M.tg = h->tg;
+  // Fcur = the next step's force field; unode = this step's node velocities
+  M.L = lbm_view<T>(h, h->cur, h->cur);
   M.f_limit = (T)h->u.f_limit;
   if (h->p.launch == HC_LAUNCH_BATCHED && all_due && h->ncells > 0) {
     M.fuse_spread = fuse ? 1 : 0;
+    M.fuse_advance = fuse && fuse_adv ? 1 : 0;
+    if (M.fuse_advance) h->stamp_ahead = true;
     size_t smem = 0;
     for (TypeSlot& ts : h->types)
       if (!ts.cells.empty()) smem = std::max(smem, mech_smem(h, ts, h->tune[6]));
@@ -650,12 +667,20 @@ int enq_step(hc_handle* h) {
     if ((rc = enq_spread<T>(h)) != HC_OK) return rc;
   }
   if ((rc = enq_collide<T>(h)) != HC_OK) return rc;
-  if ((rc = enq_interp_advance<T>(h, h->iter % h->velocity_every == 0, 1)) != HC_OK) return rc;
   const bool fuse = fusable(h);
-  // the fused spread is the next step's: its repulsion uses the positions
-  // just advanced, which are that step's positions
-  if (fuse && (rc = enq_repulsion<T>(h, h->iter + 1)) != HC_OK) return rc;
-  if ((rc = enq_mechanics<T>(h, false, fuse)) != HC_OK) return rc;
+  // without repulsion (which needs every cell advanced first) the force
+  // assembly also interpolates and advances its cell's vertices
+  const bool fuse_adv = fuse && h->rep_every == 0 && h->brep_every == 0 && (h->tune[7] & 0x800) == 0;
+  if (fuse_adv) {
+    LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
+    HC_CUDA(h, launch_nv<T>(h, L));
+  } else {
+    if ((rc = enq_interp_advance<T>(h, h->iter % h->velocity_every == 0, 1)) != HC_OK) return rc;
+    // the fused spread is the next step's: its repulsion uses the positions
+    // just advanced, which are that step's positions
+    if (fuse && (rc = enq_repulsion<T>(h, h->iter + 1)) != HC_OK) return rc;
+  }
+  if ((rc = enq_mechanics<T>(h, false, fuse, fuse_adv)) != HC_OK) return rc;
   h->spread_done = fuse;
   h->iter++;
   return HC_OK;
@@ -672,7 +697,7 @@ bool graph_eligible(hc_handle* h) {
 template <typename T>
 int build_graph(hc_handle* h, int parity) {
   const int save_cur = h->cur, save_iter = h->iter;
-  const bool save_sd = h->spread_done;
+  const bool save_sd = h->spread_done, save_sa = h->stamp_ahead;
   h->cur = parity;
   cudaGraph_t g = nullptr;
   HC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -682,6 +707,7 @@ int build_graph(hc_handle* h, int parity) {
   h->cur = save_cur;
   h->iter = save_iter;
   h->spread_done = save_sd;
+  h->stamp_ahead = save_sa;
   if (rc != HC_OK) {
     if (g) cudaGraphDestroy(g);
     return rc;
@@ -895,6 +921,7 @@ int autotune(hc_handle* h, const char* cache) {
   if (h->frep_cell) parts.push_back({h->frep_cell, 3 * h->ts * (size_t)h->rep_vcap});
   if (h->frep_wall) parts.push_back({h->frep_wall, 3 * h->ts * (size_t)h->rep_vcap});
   parts.push_back({h->status, sizeof(unsigned int)});
+  parts.push_back({h->stamp, sizeof(uint32_t)});
   size_t total = 0;
   for (auto& pr : parts) total += (pr.second + 255) / 256 * 256;
   char* snap = nullptr;
@@ -907,7 +934,7 @@ int autotune(hc_handle* h, const char* cache) {
     }
   }
   const int cur0 = h->cur, iter0 = h->iter;
-  const bool sd0 = h->spread_done;
+  const bool sd0 = h->spread_done, sa0 = h->stamp_ahead;
   auto restore = [&]() -> int {
     size_t off = 0;
     for (auto& pr : parts) {
@@ -917,6 +944,7 @@ int autotune(hc_handle* h, const char* cache) {
     h->cur = cur0;
     h->iter = iter0;
     h->spread_done = sd0;
+    h->stamp_ahead = sa0;
     return HC_OK;
   };
   cudaEvent_t ea, eb;
@@ -970,6 +998,18 @@ int autotune(hc_handle* h, const char* cache) {
   h->tune[1] = by;
   h->tune[7] = b7 | nvflags;
   if (b7 >= 2) set_bulk_plan<T>(h, b7);
+  // interpolation + advance fused into the force assembly (bit 11 turns it off)
+  {
+    const int keep = h->tune[7];
+    h->tune[7] = keep | 0x800;
+    const float t = trial();
+    if (t < best) {
+      best = t;
+      b7 |= 0x800;
+    } else {
+      h->tune[7] = keep;
+    }
+  }
   // programmatic dependent launch of the step's kernels (bit 10)
   {
     const int keep = h->tune[7];
@@ -1044,6 +1084,8 @@ int autotune(hc_handle* h, const char* cache) {
 
 template <typename T>
 int profile_stages(hc_handle* h, int nsteps, double* out) {
+  int rc0 = undo_fused_spread(h);  // every profiled step spreads on its own
+  if (rc0 != HC_OK) return rc0;
   cudaEvent_t ev[5];
   for (auto& e : ev) HC_CUDA(h, cudaEventCreate(&e));
   double acc[5] = {0, 0, 0, 0, 0};
@@ -1250,9 +1292,17 @@ int hc_set_wall_velocity(hc_handle* h, int cls, const double* u3) {
 
 int hc_set_body_force(hc_handle* h, int mode, const double* p) {
   if (!h) return HC_ERR_INVALID;
-  h->spread_done = false;  // the force field is refilled with the body force
   if (mode < HC_BODY_NONE || mode > HC_BODY_KOLMOGOROV) return fail(h, HC_ERR_INVALID, "unknown body-force mode");
   if (mode != HC_BODY_NONE && !p) return fail(h, HC_ERR_INVALID, "body-force parameters missing");
+  // the driver's setExternalVector after every iterate(): the same force again
+  // changes nothing (the reset to it is part of the collide-stream)
+  if (mode == h->body_mode &&
+      (mode == HC_BODY_NONE || (p[0] == h->body[0] && (mode == HC_BODY_KOLMOGOROV || (p[1] == h->body[1] && p[2] == h->body[2])))))
+    return HC_OK;
+  // the force field is refilled with the body force: a spread already fused
+  // into it is dropped (and the node-tag stamp caught up) first
+  int rc0 = undo_fused_spread(h);
+  if (rc0 != HC_OK) return rc0;
   h->body_mode = mode;
   for (int a = 0; a < 3; ++a) h->body[a] = (mode != HC_BODY_NONE) ? p[a] : 0.0;
   if (mode == HC_BODY_KOLMOGOROV) h->body[1] = h->body[2] = 0.0;
@@ -1606,8 +1656,9 @@ int hc_read_force_field(hc_handle* h, double* F, int which) {
 
 int hc_write_force_field(hc_handle* h, const double* F) {
   if (!h || !F) return HC_ERR_INVALID;
-  h->spread_done = false;  // the field is overwritten: it holds no spread
   int rc;
+  // the field is overwritten and holds no spread afterwards
+  if ((rc = undo_fused_spread(h)) != HC_OK) return rc;
   if ((rc = ensure_scratch(h, sizeof(double) * 3 * h->N)) != HC_OK) return rc;
   HC_CUDA(h, cudaMemcpyAsync(h->scratch, F, 8 * 3 * h->N, cudaMemcpyHostToDevice, h->stream));
   for (int k = 0; k < 2; ++k) {
@@ -1778,7 +1829,7 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
     return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather), 1 (scatter) or 2 (staged gather)");
   {
     const int mode = in8[7] & 0xff;
-    if ((in8[7] & ~0x7ff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-10 are defined");
+    if ((in8[7] & ~0xfff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-11 are defined");
     if ((in8[7] & 0x300) == 0x300) return fail(h, HC_ERR_INVALID, "tune[7]: one node-velocity variant at a time");
     if ((in8[7] & 0x200) && 19LL * h->N >= (1LL << 31))
       return fail(h, HC_ERR_INVALID, "packed node velocity needs 19 N < 2^31");

@@ -694,7 +694,7 @@ __device__ __forceinline__ void spread_vertex(const MechView<T>& M, int gi, V3t<
   if (vv.frep_wall) f = f + V3t<T>{vv.frep_wall[gi], vv.frep_wall[V + gi], vv.frep_wall[2 * V + gi]};
   Kern<T> K;
   ibm_weights(M.L, vv.x[gi], vv.x[V + gi], vv.x[2 * V + gi], K);
-  const uint32_t stamp = *M.L.stamp;
+  const uint32_t stamp = *M.L.stamp + (M.fuse_advance ? 1u : 0u);
   T* F = const_cast<T*>(M.L.Fcur);
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
@@ -702,6 +702,86 @@ __device__ __forceinline__ void spread_vertex(const MechView<T>& M, int gi, V3t<
     M.L.ntag[K.node[j]] = stamp;
     FieldLayout<T>::add(F, M.L.N, K.node[j], f.x * K.w[j], f.y * K.w[j], f.z * K.w[j]);
   }
+}
+
+// Interpolation and advance of one cell's vertices by the CTA that then
+// assembles its forces (the step's interpolate + advance stage fused in front
+// of the constitutive model): velocity from the node velocities with the
+// phi2 weights, Euler step, nearest node and tile, and the cell's deletion
+// when a vertex reaches a wall node (core/hemoCellParticleField.cpp:566-588,
+// :819-839).
+template <typename T>
+__device__ __forceinline__ void advance_cell(const MechView<T>& M, const TypeDev& t, int cell) {
+  __shared__ int hit;
+  const VertexView<T>& vv = M.vv;
+  const LbmView<T>& L = M.L;
+  const long long V = vv.V;
+  const int voff = M.cell_voff[cell];
+  if (threadIdx.x == 0) hit = 0;
+  __syncthreads();
+  const bool alive = vv.alive[cell] != 0;
+  for (int k = threadIdx.x; k < t.nv; k += blockDim.x) {
+    const int i = voff + k;
+    if (!alive) {
+      vv.vnode[i] = -1;
+      vv.vtile[i] = -1;
+      continue;
+    }
+    double px = vv.x[i], py = vv.x[V + i], pz = vv.x[2 * V + i];
+    Kern<T> K;
+    ibm_weights(L, px, py, pz, K);
+    T vx = T(0), vy = T(0), vz = T(0);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      if (K.node[j] < 0) continue;
+      T ux, uy, uz;
+      FieldLayout<T>::load(L.unode, L.N, K.node[j], ux, uy, uz);
+      vx += ux * K.w[j];
+      vy += uy * K.w[j];
+      vz += uz * K.w[j];
+    }
+    vv.v[i] = vx;
+    vv.v[V + i] = vy;
+    vv.v[2 * V + i] = vz;
+    if (!(isfinite(vx) && isfinite(vy) && isfinite(vz))) atomicOr(vv.status, STATUS_NONFINITE);
+    px += (double)vx;
+    py += (double)vy;
+    pz += (double)vz;
+    vv.x[i] = px;
+    vv.x[V + i] = py;
+    vv.x[2 * V + i] = pz;
+    const double P[3] = {px, py, pz};
+    const int dims[3] = {L.nx, L.ny, L.nz};
+    int q[3];
+    bool inside = true;
+    for (int a = 0; a < 3; ++a) {
+      long long qi = (long long)floor(P[a] + 0.5);
+      if (qi < 0 || qi >= dims[a]) {
+        if (L.per[a]) {
+          const long long mm = qi % dims[a];
+          qi = mm < 0 ? mm + dims[a] : mm;
+        } else {
+          inside = false;
+        }
+      }
+      q[a] = (int)qi;
+    }
+    if (!inside) {
+      vv.vnode[i] = -1;
+      vv.vtile[i] = -1;
+      continue;
+    }
+    const long long nd = (long long)q[0] + (long long)L.nx * ((long long)q[1] + (long long)L.ny * q[2]);
+    vv.vnode[i] = (int)nd;
+    vv.vtile[i] = q[0] / M.tg.tx + M.tg.ntx * (q[1] / M.tg.ty + M.tg.nty * (q[2] / M.tg.tz));
+    if (L.flag[nd] != 0) hit = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && hit) {
+    vv.alive[cell] = 0;
+    atomicOr(vv.status, STATUS_CELL_DELETED);
+  }
+  __syncthreads();
 }
 
 // The vertex-centric force assembly of one cell (variant 0; the staged
@@ -900,6 +980,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
     __syncthreads();  // previous cell fully written out
     if (threadIdx.x == 0) tshared = M.types[M.cell_type[cell]];
     __syncthreads();
+    if (M.fuse_advance) advance_cell(M, tshared, cell);
     gather_cell(M, tshared, cell, red, sx);
   }
   pdl_trigger();
@@ -939,6 +1020,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics_staged
     if (tid == 0) tshared = M.types[M.cell_type[cell]];
     __syncthreads();
     const TypeDev& t = tshared;
+    if (M.fuse_advance) advance_cell(M, t, cell);
     if (staged_smem_bytes<T>(t.model, t.nv, t.nf, t.ne) > (size_t)M.dyn_smem) {
       gather_cell(M, t, cell, red, sx);
       continue;

@@ -48,6 +48,10 @@ struct LbmView {
   const uint32_t* fluid;
   int nfluid;
   int pdl;  // launch the step's kernels with programmatic dependent launch
+  // collide-stream advances the node-tag stamp by one (its first thread): the
+  // spread before it was fused into the force assembly, which tags with
+  // stamp + 1 so that no CTA of that kernel writes the stamp
+  int bump_stamp;
 };
 
 // status bits shared by the kernels and hc_device_status
@@ -153,6 +157,11 @@ struct MechView {
   // new vertex force (FORCE_LIMIT-clamped) into L.Fcur and tags the stencil
   // nodes, so the next step needs no spread pass
   int fuse_spread;
+  // interpolation and advance fused in front of the force assembly: each CTA
+  // interpolates and advances its cell's vertices first (with fuse_spread,
+  // which then tags with stamp + 1)
+  int fuse_advance;
+  TileGrid tg;
   LbmView<T> L;
   T f_limit;
 };
@@ -191,6 +200,8 @@ template <typename T>
 cudaError_t launch_collide_stream_bulk(const LbmView<T>& L, const BulkPlan& P, cudaStream_t s);
 template <typename T>
 cudaError_t launch_node_velocity(const LbmView<T>& L, cudaStream_t s);
+// one increment of the node-tag stamp, in stream order
+cudaError_t launch_bump_stamp(uint32_t* stamp, cudaStream_t s);
 // the same two kernels with one thread per fluid node (L.fluid)
 template <typename T>
 cudaError_t launch_collide_stream_fluid(const LbmView<T>& L, int bs, cudaStream_t s);

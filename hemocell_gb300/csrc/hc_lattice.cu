@@ -73,6 +73,8 @@ __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z,
 template <typename T, bool ROWS, bool I32>
 __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
   pdl_wait();
+  if (L.bump_stamp && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    *L.stamp += 1;
   // I32: every population index fits 32 bits (19 N < 2^31), so interior
   // nodes pull through L.off and all index arithmetic stays 32-bit
   using Idx = typename std::conditional<I32, int, long long>::type;
@@ -122,6 +124,7 @@ __device__ __forceinline__ void unpack_node(uint32_t c, int& X, int& Y, int& Z) 
 template <typename T>
 __global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L) {
   pdl_wait();
+  if (L.bump_stamp && blockIdx.x == 0 && threadIdx.x == 0) *L.stamp += 1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= L.nfluid) return;
   int X, Y, Z;
@@ -174,6 +177,7 @@ struct StageLayout {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_collide_stream_bulk(const LbmView<T> L, const BulkPlan P) {
+  if (L.bump_stamp && blockIdx.x == 0 && threadIdx.x == 0) *L.stamp += 1;
   extern __shared__ __align__(128) unsigned char k1b_smem[];
   uint64_t* bars = reinterpret_cast<uint64_t*>(k1b_smem);
   unsigned char* stage0 = k1b_smem + 128;
@@ -640,6 +644,12 @@ __global__ void k_convert_in(const double* src, T* dst, long long n) {
 template <typename T>
 cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream_t s) {
   k_convert_in<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, dst, n);
+  return cudaGetLastError();
+}
+
+__global__ void k_bump_stamp(uint32_t* stamp) { *stamp += 1; }
+cudaError_t launch_bump_stamp(uint32_t* stamp, cudaStream_t s) {
+  k_bump_stamp<<<1, 1, 0, s>>>(stamp);
   return cudaGetLastError();
 }
 

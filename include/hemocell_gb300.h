@@ -240,7 +240,8 @@ int hc_get_tuning(hc_handle* h, int* out8);
  * (0 (x,y)-blocks or rows, 1 one thread per fluid node, else bulk copies:
  * stages | CTAs per SM << 4), bit 8 node velocity per fluid node, bit 9 node
  * velocity over warp-packed tagged nodes, bit 10 programmatic dependent launch
- * of the step's kernels */
+ * of the step's kernels, bit 11 keeps interpolation + advance a kernel of
+ * their own in the batched step (by default the force assembly does them) */
 int hc_set_tuning(hc_handle* h, const int* in8);
 
 /* --- mesh helpers (helper/meshGeneratingFunctions.hh:31-271).  Buffers are

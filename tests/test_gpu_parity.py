@@ -513,3 +513,70 @@ def test_programmatic_dependent_launch_same_results(built, form):
     assert b.device_status() == a.device_status()
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("form,launch", [(0, 0), (0, 1), (1, 1)])
+def test_odd_lattice_against_oracle(built, form, launch):
+    """A 21x17x19 lattice (no size a multiple of a block edge) with moving
+    walls in z, periodic x and y, a body force and one platelet crossing the
+    periodic x face: 60 steps against the oracle.  Exercises the pull's wrap
+    corrections, partial blocks and the platelet path."""
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    n = (21, 17, 19)
+    flags, walls = C.shear_walls(n, 3000.0)
+    t = C.plt_type(80, radius_m=1.0e-6, aspect=0.4)
+    xyz = C.place_cells(t.mesh, np.array([[20.6, 8.0, 9.0]]), np.array([[0.4, -0.3, 0.2]]))
+    case = C.Case("odd", n, (1, 1, 0), flags=flags, walls=walls, types=[t], cells=[(0, xyz)],
+                  body_mode=L.HC_BODY_UNIFORM, body=(3e-6, -2e-6, 0.0))
+    hc = case.build(form=form, launch=launch)
+    o = _orc().apply_case(case)
+    hc.iterate(60)
+    o.step(60)
+    tol = RUN_TOL if form == 0 else 1e-4
+    fluid = case.flags_array() == 0
+    assert rel_l2(hc.read_fluid()[1][:, fluid], o.read_fluid()[1][:, fluid]) < tol
+    assert rel_l2(hc.read_vertices()[0], o.read_vertices()[0]) < tol
+    assert np.array_equal(hc.read_cells()[0], o.read_cells()[0])
+    hc.close()
+
+
+def test_lattice_without_cells_batched(built):
+    """Batched stepping (graph) of a lattice with no cells, both forms."""
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    case = C.Case("empty", (24, 20, 16), (1, 1, 1), body_mode=L.HC_BODY_KOLMOGOROV, body=(1e-5, 0.0, 0.0))
+    for form in (0, 1):
+        hc = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+        o = _orc().apply_case(case)
+        hc.iterate(50)
+        o.step(50)
+        assert rel_l2(hc.read_fluid()[1], o.read_fluid()[1]) < (RUN_TOL if form == 0 else 1e-4)
+        hc.close()
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_fused_advance_same_results(built, form):
+    """Interpolation and advance inside the force assembly (the batched
+    default) against their own kernel (tune[7] bit 11), over steps with a
+    state change in between and a cell that reaches a wall."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=True)
+    out = []
+    for bit in (0, 0x800):
+        hc = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+        t = hc.tuning()
+        t[7] |= bit
+        hc.set_tuning(t)
+        hc.iterate(25)
+        hc.setExternalVector(1, (1e-6, 2e-6, 0.0))     # undoes the fused spread
+        hc.iterate(26)
+        x, v, _ = hc.read_vertices()
+        out.append((x, v, hc.read_fluid()[1], hc.read_cells()[0], hc.read_bins(), hc.device_status()))
+        hc.close()
+    tol = RUN_TOL if form == 0 else 1e-5
+    a, b = out
+    assert rel_l2(b[0], a[0]) < tol and rel_l2(b[1], a[1]) < max(tol, 1e-9) and rel_l2(b[2], a[2]) < tol
+    assert np.array_equal(a[3], b[3]) and a[5] == b[5]
+    for k in ("vertex_node", "tile_offsets", "tile_cells"):
+        assert np.array_equal(a[4][k], b[4][k]), k
