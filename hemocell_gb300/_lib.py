@@ -91,6 +91,7 @@ SIGNATURES = {
     "hc_sync": (C.c_int, [P]),
     "hc_time_steps": (C.c_int, [P, C.c_int, D]),
     "hc_profile_stages": (C.c_int, [P, C.c_int, D]),
+    "hc_profile_kernels": (C.c_int, [P, C.c_int, D]),
     "hc_read_fluid": (C.c_int, [P, D, D]),
     "hc_read_populations": (C.c_int, [P, D]),
     "hc_write_populations": (C.c_int, [P, D]),

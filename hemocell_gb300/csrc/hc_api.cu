@@ -131,6 +131,10 @@ struct hc_handle {
   // tagged the stencil nodes with stamp + 1: the next collide-stream (or a
   // state change) advances the stamp
   bool stamp_ahead = false;
+  // per-kernel profile of the step (hc_profile_kernels): while prof_step >= 0,
+  // enq_step records prof_ev[prof_step * 6 + slot] around its kernels
+  std::vector<cudaEvent_t> prof_ev;
+  int prof_step = -1;
   // external vertex forces (HemoCellStretch)
   int next = 0, next_cap = 0;
   int* ext_ids = nullptr;
@@ -243,6 +247,11 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   L.status = h->status;
   L.pdl = (h->tune[7] & 0x400) ? 1 : 0;
   L.bump_stamp = 0;
+  L.k1var = (h->tune[7] >> 12) & 3;
+  L.moving_walls = 0;
+  for (int c = 0; c < hcd::MAX_WALL_CLASSES; ++c)
+    for (int a = 0; a < 3; ++a)
+      if (h->uw[c][a] != 0.0) L.moving_walls = 1;
   L.fluid = h->nfluid > 0 ? h->fluid : nullptr;
   L.nfluid = h->nfluid;
   L.fast = 19LL * h->N < (1LL << 31) ? 1 : 0;
@@ -311,6 +320,11 @@ void build_nbmask(hc_handle* h, std::vector<uint32_t>& mask) {
         }
         uint32_t cw = cls < 0 ? 0u : (uint32_t)cls;
         if (mixed || cw >= (uint32_t)hcd::MAX_WALL_CLASSES) cw = hcd::NB_CLASS_MIXED;
+        // interior: every link pulls from the unwrapped neighbour
+        const bool face = (h->p.periodic[0] && (X == 0 || X == nx - 1)) ||
+                          (h->p.periodic[1] && (Y == 0 || Y == ny - 1)) ||
+                          (h->p.periodic[2] && (Z == 0 || Z == nz - 1));
+        if (m == 0 && !face) m |= hcd::NB_INTERIOR;
         mask[n] = m | (cw << hcd::NB_CLASS_SHIFT);
       }
 }
@@ -562,7 +576,8 @@ bool set_bulk_plan(hc_handle* h, int code) {
 template <typename T>
 int enq_interp_advance(hc_handle* h, int do_interp, int do_advance, int mark = 0) {
   LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
-  if (do_interp) {
+  // no vertex, no stencil node to evaluate (the scan alone is thousands of blocks)
+  if (do_interp && h->nvert > 0) {
     if (mark) HC_CUDA(h, hcd::launch_mark_nodes<T>(L, vertex_view<T>(h), h->stream));
     HC_CUDA(h, launch_nv<T>(h, L));
   }
@@ -618,6 +633,10 @@ size_t mech_smem(const hc_handle* h, const TypeSlot& ts, int variant) {
   return staged <= kStagedMax ? staged : gather;
 }
 
+inline void prof_mark(hc_handle* h, int slot) {
+  if (h->prof_step >= 0) cudaEventRecord(h->prof_ev[h->prof_step * 6 + slot], h->stream);
+}
+
 template <typename T>
 int enq_mechanics(hc_handle* h, bool forced, bool fuse = false, bool fuse_adv = false) {
   bool all_due = true;
@@ -666,11 +685,14 @@ int enq_step(hc_handle* h) {
     if ((rc = enq_repulsion<T>(h, h->iter)) != HC_OK) return rc;
     if ((rc = enq_spread<T>(h)) != HC_OK) return rc;
   }
+  prof_mark(h, 0);
   if ((rc = enq_collide<T>(h)) != HC_OK) return rc;
+  prof_mark(h, 1);
   const bool fuse = fusable(h);
   // without repulsion (which needs every cell advanced first) the force
   // assembly also interpolates and advances its cell's vertices
   const bool fuse_adv = fuse && h->rep_every == 0 && h->brep_every == 0 && (h->tune[7] & 0x800) == 0;
+  prof_mark(h, 2);
   if (fuse_adv) {
     LbmView<T> L = lbm_view<T>(h, h->cur, 1 - h->cur);
     HC_CUDA(h, launch_nv<T>(h, L));
@@ -680,7 +702,10 @@ int enq_step(hc_handle* h) {
     // just advanced, which are that step's positions
     if (fuse && (rc = enq_repulsion<T>(h, h->iter + 1)) != HC_OK) return rc;
   }
+  prof_mark(h, 3);
+  prof_mark(h, 4);
   if ((rc = enq_mechanics<T>(h, false, fuse, fuse_adv)) != HC_OK) return rc;
+  prof_mark(h, 5);
   h->spread_done = fuse;
   h->iter++;
   return HC_OK;
@@ -966,7 +991,10 @@ int autotune(hc_handle* h, const char* cache) {
   };
   invalidate_graph(h);
   // collide-stream: (x, y)-blocks, whole rows, one thread per fluid node, bulk copies
-  const int k1[][2] = {{0, 1}, {0, 2}, {0, 4}, {32, 4}, {64, 2}, {64, 4}, {128, 1}, {128, 2}, {256, 1}, {32, 8}};
+  // (x, y)-blocks of whole rows, and blocks whose warps are 8 x 4 or 16 x 2
+  // tiles, for which most warps away from walls hold only interior nodes
+  const int k1[][2] = {{0, 1},  {0, 2},  {0, 4},  {32, 4}, {64, 2}, {64, 4}, {128, 1}, {128, 2},
+                       {256, 1}, {32, 8}, {8, 16}, {8, 32}, {16, 8}, {16, 16}};
   const int nvflags = h->tune[7] & 0x300;
   float best = 1e30f;
   int bx = h->tune[0], by = h->tune[1], b7 = h->tune[7] & 0xff;
@@ -982,13 +1010,17 @@ int autotune(hc_handle* h, const char* cache) {
       b7 = code;
     }
   };
+  const bool fast32 = 19LL * h->N < (1LL << 31);
   for (auto& c : k1) {
     if (c[0] > 2 * h->nx && c[0] > 32) continue;
     if (c[0] == 0 && h->nx * c[1] > 256) continue;
     try_k1(c[0], c[1], 0);
+    // the interior pull (bit 12) of the direct kernel
+    if (fast32 && !(c[0] == 0 && h->nx <= 256)) try_k1(c[0], c[1], 0x1000);
   }
   if (h->nfluid > 0)
-    for (int bs : {128, 256}) try_k1(bs, 1, 1);
+    for (int bs : {128, 256})
+      for (int var : {0, 0x1000}) try_k1(bs, 1, 1 | var);
   for (int ctas : {1, 2})
     for (int st : {3, 4}) {
       const int code = st | (ctas << 4);
@@ -997,7 +1029,7 @@ int autotune(hc_handle* h, const char* cache) {
   h->tune[0] = bx;
   h->tune[1] = by;
   h->tune[7] = b7 | nvflags;
-  if (b7 >= 2) set_bulk_plan<T>(h, b7);
+  if ((b7 & 0xff) >= 2) set_bulk_plan<T>(h, b7);
   // interpolation + advance fused into the force assembly (bit 11 turns it off)
   {
     const int keep = h->tune[7];
@@ -1006,6 +1038,19 @@ int autotune(hc_handle* h, const char* cache) {
     if (t < best) {
       best = t;
       b7 |= 0x800;
+    } else {
+      h->tune[7] = keep;
+    }
+  }
+  // evict-last population stores of the direct or fluid-list collide-stream (bit 13)
+  const bool direct = (b7 & 0xff) == 0 && fast32 && !(h->tune[0] == 0 && h->nx <= 256);
+  if (direct || (b7 & 0xff) == 1) {
+    const int keep = h->tune[7];
+    h->tune[7] = keep | 0x2000;
+    const float t = trial();
+    if (t < best) {
+      best = t;
+      b7 |= 0x2000;
     } else {
       h->tune[7] = keep;
     }
@@ -1112,6 +1157,48 @@ int profile_stages(hc_handle* h, int nsteps, double* out) {
   }
   for (auto& e : ev) cudaEventDestroy(e);
   for (int s = 0; s < 5; ++s) out[s] = nsteps > 0 ? acc[s] / nsteps : 0.0;
+  return HC_OK;
+}
+
+// Device time of each kernel group inside the step as hc_step runs it in
+// the batched launch (the same kernels and fusions as the graph), launched
+// one after another without a graph: three unprofiled steps are queued
+// first and nothing synchronises in between, so the host stays ahead of the
+// GPU and no launch gap falls between a kernel's two events.
+// out[0] collide-stream, out[1] node velocity (or interpolation + advance
+// when not fused), out[2] force assembly, out[3] whole step, in ms per step.
+template <typename T>
+int profile_kernels(hc_handle* h, int nsteps, double* out) {
+  int rc;
+  if (h->prof_ev.size() < (size_t)nsteps * 6) {
+    for (auto e : h->prof_ev) cudaEventDestroy(e);
+    h->prof_ev.assign((size_t)nsteps * 6, nullptr);
+    for (auto& e : h->prof_ev) HC_CUDA(h, cudaEventCreate(&e));
+  }
+  for (int k = 0; k < 3; ++k)
+    if ((rc = enq_step<T>(h)) != HC_OK) return rc;
+  for (int k = 0; k < nsteps; ++k) {
+    h->prof_step = k;
+    rc = enq_step<T>(h);
+    h->prof_step = -1;
+    if (rc != HC_OK) return rc;
+  }
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  double acc[4] = {0, 0, 0, 0};
+  for (int k = 0; k < nsteps; ++k) {
+    cudaEvent_t* e = &h->prof_ev[(size_t)k * 6];
+    float t;
+    for (int g = 0; g < 3; ++g) {
+      HC_CUDA(h, cudaEventElapsedTime(&t, e[2 * g], e[2 * g + 1]));
+      acc[g] += t;
+    }
+    if (k + 1 < nsteps) {
+      HC_CUDA(h, cudaEventElapsedTime(&t, e[0], e[6]));
+      acc[3] += t;
+    }
+  }
+  for (int g = 0; g < 3; ++g) out[g] = nsteps > 0 ? acc[g] / nsteps : 0.0;
+  out[3] = nsteps > 1 ? acc[3] / (nsteps - 1) : 0.0;
   return HC_OK;
 }
 
@@ -1251,6 +1338,7 @@ int hc_destroy(hc_handle* h) {
                   h->ext_ids, h->ext_f, h->rep_cnt, h->rep_slot, h->rep_vq, h->rep_xr, h->rep_bnode,
                   h->frep_cell, h->frep_wall, h->fluid};
   for (void* q : ptrs) dfree(h, q);
+  for (auto e : h->prof_ev) cudaEventDestroy(e);
   if (h->pool) release_pool(h->p.device, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1604,6 +1692,11 @@ int hc_profile_stages(hc_handle* h, int nsteps, double* ms5) {
   return h->f64 ? profile_stages<double>(h, nsteps, ms5) : profile_stages<float>(h, nsteps, ms5);
 }
 
+int hc_profile_kernels(hc_handle* h, int nsteps, double* ms4) {
+  if (!h || !ms4 || nsteps < 1 || nsteps > 100000) return HC_ERR_INVALID;
+  return h->f64 ? profile_kernels<double>(h, nsteps, ms4) : profile_kernels<float>(h, nsteps, ms4);
+}
+
 int hc_read_fluid(hc_handle* h, double* rho, double* u) {
   if (!h) return HC_ERR_INVALID;
   int rc;
@@ -1819,8 +1912,13 @@ int hc_get_tuning(hc_handle* h, int* out8) {
 
 int hc_set_tuning(hc_handle* h, const int* in8) {
   if (!h || !in8) return HC_ERR_INVALID;
-  if (in8[0] < 0 || in8[1] <= 0 || in8[0] * in8[1] > 256 || in8[0] % 32 != 0)
-    return fail(h, HC_ERR_INVALID, "collide-stream block must be 0 (whole rows) or a multiple of 32 wide, at most 256 threads");
+  // width 0 (whole rows), a multiple of 32, or 8 / 16 (warps as 8 x 4 or 16 x 2
+  // tiles); whole warps, at most 256 threads
+  const bool width_ok = in8[0] == 0 || in8[0] % 32 == 0 || in8[0] == 8 || in8[0] == 16;
+  if (in8[0] < 0 || in8[1] <= 0 || in8[0] * in8[1] > 256 || !width_ok || (in8[0] > 0 && in8[0] * in8[1] % 32 != 0))
+    return fail(h, HC_ERR_INVALID,
+                "collide-stream block must be 0 (whole rows), 8, 16 or a multiple of 32 wide, whole warps, "
+                "at most 256 threads");
   for (int k = 2; k <= 3; ++k)
     if (in8[k] <= 0 || in8[k] > 512 || in8[k] % 32 != 0) return fail(h, HC_ERR_INVALID, "bad block size");
   if (in8[4] <= 0 || in8[4] > (h->f64 ? 384 : 768) || in8[4] % 32 != 0)
@@ -1829,7 +1927,7 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
     return fail(h, HC_ERR_INVALID, "mechanics variant is 0 (gather), 1 (scatter) or 2 (staged gather)");
   {
     const int mode = in8[7] & 0xff;
-    if ((in8[7] & ~0xfff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-11 are defined");
+    if ((in8[7] & ~0x3fff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-13 are defined");
     if ((in8[7] & 0x300) == 0x300) return fail(h, HC_ERR_INVALID, "tune[7]: one node-velocity variant at a time");
     if ((in8[7] & 0x200) && 19LL * h->N >= (1LL << 31))
       return fail(h, HC_ERR_INVALID, "packed node velocity needs 19 N < 2^31");

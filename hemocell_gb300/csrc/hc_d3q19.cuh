@@ -52,6 +52,27 @@ __device__ __forceinline__ T cdot(int cx, int cy, int cz, T x, T y, T z) {
   return r;
 }
 
+// Population stores with an L2::evict_last cache policy (KEEP): the buffer a
+// collide-stream writes is read next by the node-velocity pass and the next
+// collide-stream, while the buffer it reads is dead once pulled, so the
+// written lines are the ones worth keeping in the 129 MB L2.
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void st_policy(float* p, float v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_policy(double* p, double v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(v), "l"(pol) : "memory");
+}
+template <bool KEEP, typename T>
+__device__ __forceinline__ void st_pop(T* p, T v, uint64_t pol) {
+  if constexpr (KEEP) st_policy(p, v, pol);
+  else *p = v;
+}
+
 // Force-field layout: FP32 keeps one float4 (Fx, Fy, Fz, 0) per node so a
 // spread contribution is a single vector atomic; FP64 keeps [3][N].
 template <typename T>
@@ -165,7 +186,9 @@ __device__ __forceinline__ bool pull_is_inline(const LbmView<T>&, int, int, int,
 // the node's own opposite population instead (one load either way) and takes
 // the moving-wall term of its class, so the lanes of a warp at a wall or on
 // a face of the lattice do not diverge into the general pull.
-template <typename T>
+// MW = false compiles out the moving-wall term (every wall class at rest:
+// the term is then zero and the result the same).
+template <typename T, bool MW = true>
 __device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __restrict__ src, int n, int X, int Y, int Z,
                                             uint32_t m, T f[19]) {
   const int N = (int)L.N, nx = L.nx, nxy = L.nx * L.ny;
@@ -174,7 +197,12 @@ __device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __rest
   const int cym = Y == 0 ? nxy : 0, cyp = Y == L.ny - 1 ? -nxy : 0;
   const int czm = Z == 0 ? N : 0, czp = Z == L.nz - 1 ? -N : 0;
   const uint32_t cls = (m >> NB_CLASS_SHIFT) & (MAX_WALL_CLASSES - 1);
-  const T ux = L.uw[cls][0], uy = L.uw[cls][1], uz = L.uw[cls][2];
+  T ux = T(0), uy = T(0), uz = T(0);
+  if constexpr (MW) {
+    ux = L.uw[cls][0];
+    uy = L.uw[cls][1];
+    uz = L.uw[cls][2];
+  }
   f[0] = __ldg(src + n);
 #pragma unroll
   for (int j = 1; j < 19; ++j) {
@@ -183,9 +211,21 @@ __device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __rest
     const int corr = (cxi(j) > 0 ? cxm : (cxi(j) < 0 ? cxp : 0)) + (cyi(j) > 0 ? cym : (cyi(j) < 0 ? cyp : 0)) +
                      (czi(j) > 0 ? czm : (czi(j) < 0 ? czp : 0));
     const T v = __ldg(src + (bb ? i * N + n : n + L.off[j] + corr));
-    const T cuw = T(cxi(i)) * ux + T(cyi(i)) * uy + T(czi(i)) * uz;
-    f[j] = bb ? v - T(6.0 * wi(i)) * cuw : v;
+    if constexpr (MW) {
+      const T cuw = T(cxi(i)) * ux + T(cyi(i)) * uy + T(czi(i)) * uz;
+      f[j] = bb ? v - T(6.0 * wi(i)) * cuw : v;
+    } else {
+      f[j] = v;
+    }
   }
+}
+
+// Pull of an interior node (NB_INTERIOR: no bounce-back link, on no
+// periodic face, 19 N < 2^31): population j is fsrc[n + off[j]].
+template <typename T>
+__device__ __forceinline__ void pull_interior(const LbmView<T>& L, const T* __restrict__ src, int n, T f[19]) {
+#pragma unroll
+  for (int j = 0; j < 19; ++j) f[j] = __ldg(src + n + L.off[j]);
 }
 
 // rhoBar = sum f, j = sum c f over the shifted populations, pair-wise

@@ -14,7 +14,8 @@
 
 namespace hcd {
 
-constexpr uint32_t NB_SOLID = 1u << 23;  // node itself is a wall node
+constexpr uint32_t NB_SOLID = 1u << 23;     // node itself is a wall node
+constexpr uint32_t NB_INTERIOR = 1u << 22;  // fluid, no bounce-back link, on no periodic face
 constexpr int NB_CLASS_SHIFT = 24;        // wall class of the bounce-back neighbours
 constexpr uint32_t NB_CLASS_MIXED = 255;  // neighbours of differing wall class
 constexpr int MAX_WALL_CLASSES = 16;
@@ -52,6 +53,11 @@ struct LbmView {
   // spread before it was fused into the force assembly, which tags with
   // stamp + 1 so that no CTA of that kernel writes the stamp
   int bump_stamp;
+  // variant of the direct collide-stream: bit 0 interior nodes (NB_INTERIOR)
+  // pull through the plain offsets, skipping the bounce-back and wrap
+  // selects; bit 1 the populations it writes carry an L2 evict-last policy
+  int k1var;
+  int moving_walls;  // some wall class moves (else the moving-wall term is compiled out)
 };
 
 // status bits shared by the kernels and hc_device_status
@@ -165,6 +171,7 @@ struct MechView {
   LbmView<T> L;
   T f_limit;
 };
+
 
 // Kernel launch with or without programmatic dependent launch (the kernel
 // then starts with pdl_wait, see hc_async.cuh).

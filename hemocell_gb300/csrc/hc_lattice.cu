@@ -17,9 +17,11 @@ namespace hcd {
 // Guo-forced BGK collision of one node from its pulled populations f and
 // force F; writes the post-collision populations and the node's next force
 // (the body force of plane Z).
-template <typename T, typename Idx>
+template <typename T, typename Idx, bool KEEP = false>
 __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z, const T f[19], T Fx, T Fy, T Fz) {
   const Idx N = (Idx)L.N;
+  uint64_t pol = 0;
+  if constexpr (KEEP) pol = l2_policy_evict_last();
   T rhoBar, jx, jy, jz;
   moments(f, rhoBar, jx, jy, jz);
   const T rho = T(1) + rhoBar;
@@ -43,7 +45,7 @@ __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z,
   const T Aw2 = T(0.5) * Aw1, Bw2 = T(0.5) * Bw1, Gw2 = T(0.5) * Gw1, Hw2 = T(0.5) * Hw1, Kw2 = T(0.5) * Kw1,
           Lw2 = T(0.5) * Lw1;
 
-  L.fdst[n] = om1 * f[0] + T(1.0 / 3.0) * (om * A + G);
+  st_pop<KEEP>(L.fdst + n, om1 * f[0] + T(1.0 / 3.0) * (om * A + G), pol);
 #pragma unroll
   for (int i = 1; i <= 9; ++i) {
     const int j = i + 9;  // c = c_j
@@ -54,8 +56,8 @@ __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z,
     const T Hw = axis ? Hw1 : Hw2, Kw = axis ? Kw1 : Kw2, Lw = axis ? Lw1 : Lw2;
     const T P = (Bw * (cu * cu) + Aw) + (Hw * (cu * cF) + Gw);
     const T Q = Kw * cu + Lw * cF;
-    L.fdst[j * N + n] = om1 * f[j] + (P + Q);
-    L.fdst[i * N + n] = om1 * f[i] + (P - Q);
+    st_pop<KEEP>(L.fdst + j * N + n, om1 * f[j] + (P + Q), pol);
+    st_pop<KEEP>(L.fdst + i * N + n, om1 * f[i] + (P - Q), pol);
   }
   FieldLayout<T>::store(L.Fnext, N, n, L.bodyz[Z], L.bodyz[L.nz + Z], L.bodyz[2 * L.nz + Z]);
 }
@@ -70,7 +72,10 @@ __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z,
 // (pull_rows); otherwise each thread pulls directly from global memory.
 // The sweep direction alternates every step (L.reverse): a pass then starts
 // on the planes the previous pass wrote last, which are still in L2.
-template <typename T, bool ROWS, bool I32>
+// V (direct pull with I32 only): bit 0 interior nodes take pull_interior,
+// bit 1 evict-last population stores, bit 2 moving walls (clear: every wall
+// class is at rest and pull_inline drops the moving-wall term).
+template <typename T, bool ROWS, bool I32, int V = 4>
 __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
   pdl_wait();
   if (L.bump_stamp && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
@@ -100,12 +105,13 @@ __global__ void __launch_bounds__(256) k_collide_stream(const LbmView<T> L) {
     n = (Idx)X + (Idx)L.nx * ((Idx)Y + (Idx)L.ny * Z);
     m = __ldg(L.nbmask + n);
     if (m & NB_SOLID) return;
-    if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, (int)n, X, Y, Z, m, f);
+    if (I32 && (V & 1) && (m & NB_INTERIOR)) pull_interior(L, L.fsrc, (int)n, f);
+    else if (I32 && pull_is_inline(L, X, Y, Z, m)) pull_inline<T, (V & 4) != 0>(L, L.fsrc, (int)n, X, Y, Z, m, f);
     else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   }
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, N, n, Fx, Fy, Fz);
-  collide_store<T, Idx>(L, n, Z, f, Fx, Fy, Fz);
+  collide_store<T, Idx, (V & 2) != 0>(L, n, Z, f, Fx, Fy, Fz);
   pdl_trigger();
 }
 
@@ -121,7 +127,9 @@ __device__ __forceinline__ void unpack_node(uint32_t c, int& X, int& Y, int& Z) 
   Z = (int)(c >> 20);
 }
 
-template <typename T>
+// V as for k_collide_stream (bit 0 interior pull, bit 1 evict-last stores,
+// bit 2 moving walls).
+template <typename T, int V>
 __global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L) {
   pdl_wait();
   if (L.bump_stamp && blockIdx.x == 0 && threadIdx.x == 0) *L.stamp += 1;
@@ -132,11 +140,12 @@ __global__ void __launch_bounds__(256) k_collide_stream_fluid(const LbmView<T> L
   const int n = X + L.nx * (Y + L.ny * Z);
   const uint32_t m = __ldg(L.nbmask + n);
   T f[19];
-  if (pull_is_inline(L, X, Y, Z, m)) pull_inline(L, L.fsrc, n, X, Y, Z, m, f);
+  if ((V & 1) && (m & NB_INTERIOR)) pull_interior(L, L.fsrc, n, f);
+  else if (pull_is_inline(L, X, Y, Z, m)) pull_inline<T, (V & 4) != 0>(L, L.fsrc, n, X, Y, Z, m, f);
   else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T Fx, Fy, Fz;
   FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
-  collide_store<T, int>(L, n, Z, f, Fx, Fy, Fz);
+  collide_store<T, int, (V & 2) != 0>(L, n, Z, f, Fx, Fy, Fz);
   pdl_trigger();
 }
 
@@ -144,7 +153,17 @@ template <typename T>
 cudaError_t launch_collide_stream_fluid(const LbmView<T>& L, int bs, cudaStream_t s) {
   if (L.nfluid <= 0) return cudaSuccess;
   if (bs <= 0 || bs > 256) bs = 256;
-  return launch_kernel(k_collide_stream_fluid<T>, dim3((L.nfluid + bs - 1) / bs), dim3(bs), 0, s, L.pdl, L);
+  const dim3 g((L.nfluid + bs - 1) / bs), b(bs);
+  switch ((L.k1var & 3) | (L.moving_walls ? 4 : 0)) {
+    case 0: return launch_kernel(k_collide_stream_fluid<T, 0>, g, b, 0, s, L.pdl, L);
+    case 1: return launch_kernel(k_collide_stream_fluid<T, 1>, g, b, 0, s, L.pdl, L);
+    case 2: return launch_kernel(k_collide_stream_fluid<T, 2>, g, b, 0, s, L.pdl, L);
+    case 3: return launch_kernel(k_collide_stream_fluid<T, 3>, g, b, 0, s, L.pdl, L);
+    case 5: return launch_kernel(k_collide_stream_fluid<T, 5>, g, b, 0, s, L.pdl, L);
+    case 6: return launch_kernel(k_collide_stream_fluid<T, 6>, g, b, 0, s, L.pdl, L);
+    case 7: return launch_kernel(k_collide_stream_fluid<T, 7>, g, b, 0, s, L.pdl, L);
+    default: return launch_kernel(k_collide_stream_fluid<T, 4>, g, b, 0, s, L.pdl, L);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -351,7 +370,18 @@ cudaError_t launch_collide_stream(const LbmView<T>& L, int bx, int by, cudaStrea
   if (bx <= 0) bx = 64;
   dim3 block(bx, by, 1);
   dim3 grid((L.nx + bx - 1) / bx, (L.ny + by - 1) / by, L.nz);
-  if (L.fast) return launch_kernel(k_collide_stream<T, false, true>, grid, block, 0, s, L.pdl, L);
+  if (L.fast) {
+    switch ((L.k1var & 3) | (L.moving_walls ? 4 : 0)) {
+      case 0: return launch_kernel(k_collide_stream<T, false, true, 0>, grid, block, 0, s, L.pdl, L);
+      case 1: return launch_kernel(k_collide_stream<T, false, true, 1>, grid, block, 0, s, L.pdl, L);
+      case 2: return launch_kernel(k_collide_stream<T, false, true, 2>, grid, block, 0, s, L.pdl, L);
+      case 3: return launch_kernel(k_collide_stream<T, false, true, 3>, grid, block, 0, s, L.pdl, L);
+      case 5: return launch_kernel(k_collide_stream<T, false, true, 5>, grid, block, 0, s, L.pdl, L);
+      case 6: return launch_kernel(k_collide_stream<T, false, true, 6>, grid, block, 0, s, L.pdl, L);
+      case 7: return launch_kernel(k_collide_stream<T, false, true, 7>, grid, block, 0, s, L.pdl, L);
+      default: return launch_kernel(k_collide_stream<T, false, true, 4>, grid, block, 0, s, L.pdl, L);
+    }
+  }
   return launch_kernel(k_collide_stream<T, false, false>, grid, block, 0, s, L.pdl, L);
 }
 

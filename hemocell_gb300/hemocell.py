@@ -289,6 +289,14 @@ class HemoCell:
         self._check(self._lib.hc_profile_stages(self._h, nsteps, _dp(out)))
         return dict(zip(("spread", "collide_stream", "interp_advance", "mechanics", "step"), out.tolist()))
 
+    def profile_kernels(self, nsteps: int) -> dict:
+        """Device time (ms per step) of each kernel inside the batched step as
+        iterate runs it: collide-stream, node velocity (or interpolation +
+        advance when unfused), force assembly, whole step."""
+        out = np.zeros(4)
+        self._check(self._lib.hc_profile_kernels(self._h, nsteps, _dp(out)))
+        return dict(zip(("collide_stream", "node_velocity", "mechanics", "step"), out.tolist()))
+
     def read_positions(self, out: Optional[np.ndarray] = None):
         """Positions only, into a caller-owned (V,3) float64 buffer (pinned for
         speed), or a new array when none is given."""

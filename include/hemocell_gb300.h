@@ -154,6 +154,13 @@ int hc_sync(hc_handle* h);
  * {spread, collide_stream, interpolate+advance, mechanics, whole step} in ms */
 int hc_time_steps(hc_handle* h, int nsteps, double* ms);
 int hc_profile_stages(hc_handle* h, int nsteps, double* ms5);
+/* per-kernel device time inside the step as hc_step runs it in the batched
+ * launch (same kernels and fusions as its CUDA graph, launched without the
+ * graph and queued ahead so that no launch gap is timed): 3 unprofiled steps,
+ * then nsteps (1..100000) profiled; ms4 = mean per step of {collide-stream,
+ * node velocity (interpolation + advance when they are not fused),
+ * force assembly, whole step} */
+int hc_profile_kernels(hc_handle* h, int nsteps, double* ms4);
 
 /* --- readback (io/FluidHdf5IO.hh velocity/density, io/ParticleHdf5IO.cpp) */
 int hc_read_fluid(hc_handle* h, double* rho, double* u);        /* rho[N], u[3][N] */
@@ -227,13 +234,17 @@ int hc_load_checkpoint(hc_handle* h, const char* dir);
 int hc_get_stats(hc_handle* h, hc_stats* out);
 /* device status word, sticky: bit0 non-finite vertex velocity, bit1 cell
  * deleted at a wall, bit2 a shared-memory pipeline wait of the bulk-copy
- * collide-stream timed out (the step's results are then invalid) */
+ * collide-stream timed out (the step's results are then invalid), bit3 a
+ * lattice node held more repulsion candidates than its slots (pairs were
+ * dropped) */
 int hc_device_status(hc_handle* h, unsigned int* status);
 
 /* --- launch tuning (project autotuner; results cached on disk) */
 int hc_autotune(hc_handle* h, const char* cache_path);
 int hc_get_tuning(hc_handle* h, int* out8);
-/* in8: collide-stream block (bx, by; bx = 0 whole rows), spread block,
+/* in8: collide-stream block (bx, by; bx = 0 whole rows, else 8 or 16, whose
+ * warps are 8 x 4 or 16 x 2 tiles, or a multiple of 32; whole warps, at most
+ * 256 threads), spread block,
  * interpolation block, mechanics block, mechanics grid (0 = one CTA per cell),
  * mechanics variant (0 vertex gather, 1 face/edge scatter, 2 staged face/edge
  * terms gathered per vertex), and in8[7]: bits 0-7 the collide-stream kind
@@ -241,7 +252,11 @@ int hc_get_tuning(hc_handle* h, int* out8);
  * stages | CTAs per SM << 4), bit 8 node velocity per fluid node, bit 9 node
  * velocity over warp-packed tagged nodes, bit 10 programmatic dependent launch
  * of the step's kernels, bit 11 keeps interpolation + advance a kernel of
- * their own in the batched step (by default the force assembly does them) */
+ * their own in the batched step (by default the force assembly does them),
+ * and variants of the direct (x,y)-block and fluid-node collide-stream:
+ * bit 12 interior nodes (no bounce-back link, on no periodic face) pull
+ * through plain offsets, bit 13 the populations it writes carry an L2
+ * evict-last policy */
 int hc_set_tuning(hc_handle* h, const int* in8);
 
 /* --- mesh helpers (helper/meshGeneratingFunctions.hh:31-271).  Buffers are

@@ -515,6 +515,74 @@ def test_programmatic_dependent_launch_same_results(built, form):
     b.close()
 
 
+@pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("shape,var", [((32, 4), 0x1000), ((32, 4), 0x2000), ((8, 16), 0x3000), ((16, 8), 0x1000),
+                                       ((64, 2), 0x2000), ((256, 1), 1 | 0x3000), ((128, 1), 1 | 0x2000)])
+@pytest.mark.parametrize("walls", ["moving", "static", "odd"])
+def test_collide_stream_variants_same_bits(built, form, shape, var, walls):
+    """The direct collide-stream variants compute the same bits as the
+    whole-row kernel, over graph-replayed steps with cells: the interior pull
+    (tune[7] bit 12), evict-last population stores (bit 13), warps shaped as
+    8 x 4 and 16 x 2 tiles, one thread per fluid node (kind 1) with the interior
+    pull and evict-last stores, with moving walls (a sheared box with the moving-wall
+    term), with walls at rest (a small pipe, the term compiled out) and on a
+    21 x 17 x 19 lattice (no size a multiple of a block or column length)."""
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    if walls == "moving":
+        case = mixed_box(wall=True)
+    elif walls == "static":
+        case = C.pipe_ht25(nx=24, ny=24, nz=32, radius=10.0, n_cells=4, seed=3)
+    else:
+        n = (21, 17, 19)
+        flags, wl = C.shear_walls(n, 3000.0)
+        t = C.plt_type(80, radius_m=1.0e-6, aspect=0.4)
+        xyz = C.place_cells(t.mesh, np.array([[20.6, 8.0, 9.0]]), np.array([[0.4, -0.3, 0.2]]))
+        case = C.Case("odd", n, (1, 1, 0), flags=flags, walls=wl, types=[t], cells=[(0, xyz)],
+                      body_mode=L.HC_BODY_UNIFORM, body=(3e-6, -2e-6, 0.0))
+    a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    t = a.tuning()
+    t[0], t[1] = 0, 1
+    t[7] &= ~0xf0ff
+    a.set_tuning(t)
+    t[0], t[1] = shape
+    t[7] |= var
+    b.set_tuning(t)
+    assert b.tuning()[7] & 0xf0ff == var
+    a.iterate(30)
+    b.iterate(30)
+    assert np.array_equal(b.read_vertices()[0], a.read_vertices()[0])
+    assert np.array_equal(b.read_fluid()[1], a.read_fluid()[1])
+    assert b.device_status() == a.device_status()
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_profile_kernels_times_the_step(built, form):
+    """hc_profile_kernels runs the step hc_step runs: the state it leaves is
+    the state of as many plain steps (3 queued + nsteps), and its kernel
+    times are positive and fit inside the whole-step time."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=True)
+    a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    a.iterate(5)
+    b.iterate(5)
+    k = b.profile_kernels(10)
+    a.iterate(13)
+    tol = RUN_TOL if form == 0 else 1e-5
+    assert rel_l2(b.read_vertices()[0], a.read_vertices()[0]) < tol
+    assert rel_l2(b.read_fluid()[1], a.read_fluid()[1]) < tol
+    assert all(k[g] > 0 for g in ("collide_stream", "node_velocity", "mechanics", "step"))
+    assert k["collide_stream"] + k["node_velocity"] + k["mechanics"] <= 1.05 * k["step"] + 1e-3
+    with pytest.raises(Exception):
+        b.profile_kernels(0)
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("form,launch", [(0, 0), (0, 1), (1, 1)])
 def test_odd_lattice_against_oracle(built, form, launch):
     """A 21x17x19 lattice (no size a multiple of a block edge) with moving
