@@ -144,23 +144,31 @@ def time_form(case, form, launch, steps, warmup, tune_cache):
 
 def e2e_form(case, form, launch, steps, warmup):
     """Same metric through the public API with host buffers: every step the
-    host sets the body force (setExternalVector) from host memory, iterates,
-    and reads the vertex positions back into a pinned host buffer."""
+    host sets the body force (setExternalVector, which copies the per-plane
+    profile to the device from pinned memory), iterates, and starts copying
+    the positions into one of two pinned host buffers; the copy of step k
+    runs on its own stream during step k+1, and the host waits for it before
+    that buffer is used again (the last one is waited for inside the timed
+    region too)."""
     import torch
     from hemocell_gb300 import _lib as L
     hc = case.build(form=form, launch=launch)
     V = hc.stats().vertices
-    pos = torch.empty((V, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pos = [torch.empty((V, 3), dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
     body = np.array(case.body, np.float64)
-    for _ in range(warmup):
-        hc.setExternalVector(case.body_mode, body)
-        hc.iterate(1)
-        hc.read_positions(pos)
+
+    def run(n):
+        for k in range(n):
+            hc.setExternalVector(case.body_mode, body)
+            hc.iterate(1)
+            hc.read_positions_async(pos[k & 1], k & 1)
+            if k >= 1:
+                hc.wait_positions((k - 1) & 1)
+        hc.wait_positions((n - 1) & 1)
+
+    run(warmup)
     t0 = time.perf_counter()
-    for _ in range(steps):
-        hc.setExternalVector(case.body_mode, body)
-        hc.iterate(1)
-        hc.read_positions(pos)
+    run(steps)
     dt = time.perf_counter() - t0
     hc.close()
     h2d = 3 * case.dims[2] * (4 if form == L.HC_FORM_MIXED_F32 else 8)

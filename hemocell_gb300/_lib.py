@@ -92,6 +92,9 @@ SIGNATURES = {
     "hc_time_steps": (C.c_int, [P, C.c_int, D]),
     "hc_profile_stages": (C.c_int, [P, C.c_int, D]),
     "hc_profile_kernels": (C.c_int, [P, C.c_int, D]),
+    "hc_read_positions_async": (C.c_int, [P, D, C.c_int]),
+    "hc_wait_positions": (C.c_int, [P, C.c_int]),
+    "hc_vertex_count": (C.c_int, [P]),
     "hc_read_fluid": (C.c_int, [P, D, D]),
     "hc_read_populations": (C.c_int, [P, D]),
     "hc_write_populations": (C.c_int, [P, D]),

@@ -118,6 +118,8 @@ struct hc_handle {
   hcd::BulkPlan bulk{};
   int bulk_key = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // one-step graphs (iterate(1)), per buffer parity, built on first use
+  cudaGraphExec_t graph1[2] = {nullptr, nullptr};
   bool graph_valid = false;
   long long device_bytes = 0;
   cudaMemPool_t pool = nullptr;  // this device's library pool (all allocations)
@@ -131,6 +133,20 @@ struct hc_handle {
   // tagged the stencil nodes with stamp + 1: the next collide-stream (or a
   // state change) advances the stamp
   bool stamp_ahead = false;
+  // body-force profile staging: pinned, mapped host [profile 3 nz | change
+  // 3 nz] of T (and its device address), the device copy of the change, and
+  // the event of the last upload
+  void* hbody_pin = nullptr;
+  void* hbody_dev = nullptr;
+  void* bodyd = nullptr;
+  cudaEvent_t body_copied = nullptr;
+  // asynchronous position readback (hc_read_positions_async): a copy stream,
+  // two device staging buffers of [V][3] doubles and their events
+  cudaStream_t copy_stream = nullptr;
+  double* pos_stage[2] = {nullptr, nullptr};
+  long long pos_stage_v = 0;
+  cudaEvent_t pos_ready[2] = {nullptr, nullptr}, pos_copied[2] = {nullptr, nullptr};
+  bool pos_inflight[2] = {false, false};
   // per-kernel profile of the step (hc_profile_kernels): while prof_step >= 0,
   // enq_step records prof_ev[prof_step * 6 + slot] around its kernels
   std::vector<cudaEvent_t> prof_ev;
@@ -214,6 +230,11 @@ void dfree(hc_handle* h, void* p) {
 }
 
 void invalidate_graph(hc_handle* h) {
+  for (int k = 0; k < 2; ++k)
+    if (h->graph1[k]) {
+      cudaGraphExecDestroy(h->graph1[k]);
+      h->graph1[k] = nullptr;
+    }
   for (int k = 0; k < 2; ++k)
     if (h->graph[k]) {
       cudaGraphExecDestroy(h->graph[k]);
@@ -359,7 +380,8 @@ int upload_flags(hc_handle* h) {
   return HC_OK;
 }
 
-int upload_body(hc_handle* h) {
+// The per-plane body-force profile of the current body force (3 x nz).
+std::vector<double> body_profile(const hc_handle* h) {
   std::vector<double> bz(3 * h->nz, 0.0);
   for (int z = 0; z < h->nz; ++z) {
     if (h->body_mode == HC_BODY_UNIFORM) {
@@ -368,19 +390,52 @@ int upload_body(hc_handle* h) {
       bz[z] = h->body[0] * std::sin(2.0 * M_PI * (double)z / (double)h->nz);
     }
   }
+  return bz;
+}
+
+// Copies the profile (and, when given, its change) to the device from the
+// handle's pinned staging buffer, in the order of the handle's stream.  A
+// kernel reads the mapped buffer, so the upload does not queue on a copy
+// engine behind an asynchronous position readback.
+int upload_profile(hc_handle* h, const std::vector<double>& prof, const std::vector<double>* change) {
+  const size_t n = 3 * (size_t)h->nz;
+  if (!h->hbody_pin) {
+    HC_CUDA(h, cudaHostAlloc(&h->hbody_pin, 2 * n * h->ts, cudaHostAllocMapped));
+    HC_CUDA(h, cudaHostGetDevicePointer(&h->hbody_dev, h->hbody_pin, 0));
+    HC_CUDA(h, cudaEventCreateWithFlags(&h->body_copied, cudaEventDisableTiming));
+  } else {
+    HC_CUDA(h, cudaEventSynchronize(h->body_copied));  // the last upload has left the buffer
+  }
+  for (size_t k = 0; k < n; ++k) {
+    const double c = change ? (*change)[k] : 0.0;
+    if (h->f64) {
+      static_cast<double*>(h->hbody_pin)[k] = prof[k];
+      static_cast<double*>(h->hbody_pin)[n + k] = c;
+    } else {
+      static_cast<float*>(h->hbody_pin)[k] = (float)prof[k];
+      static_cast<float*>(h->hbody_pin)[n + k] = (float)c;
+    }
+  }
+  HC_CUDA(h, hcd::launch_copy_words(h->bodyz, h->hbody_dev, n * h->ts, h->stream));
+  if (change) {
+    if (!h->bodyd) HC_CUDA(h, dalloc(h, &h->bodyd, n * h->ts));
+    HC_CUDA(h, hcd::launch_copy_words(h->bodyd, static_cast<char*>(h->hbody_dev) + n * h->ts, n * h->ts, h->stream));
+  }
+  HC_CUDA(h, cudaEventRecord(h->body_copied, h->stream));
+  return HC_OK;
+}
+
+// Uploads the body-force profile and refills the next step's force field with it.
+int upload_body(hc_handle* h) {
+  int rc;
+  if ((rc = upload_profile(h, body_profile(h), nullptr)) != HC_OK) return rc;
   const long long plane = (long long)h->nx * h->ny;
-  if (h->f64) {
-    HC_CUDA(h, cudaMemcpyAsync(h->bodyz, bz.data(), 8 * bz.size(), cudaMemcpyHostToDevice, h->stream));
+  if (h->f64)
     HC_CUDA(h, hcd::launch_fill_body<double>((double*)h->F[h->cur], (const double*)h->bodyz, plane, h->nz, h->N,
                                              h->stream));
-  } else {
-    std::vector<float> bf(bz.begin(), bz.end());
-    HC_CUDA(h, cudaMemcpyAsync(h->bodyz, bf.data(), 4 * bf.size(), cudaMemcpyHostToDevice, h->stream));
+  else
     HC_CUDA(h, hcd::launch_fill_body<float>((float*)h->F[h->cur], (const float*)h->bodyz, plane, h->nz, h->N,
                                             h->stream));
-    // the pageable source of an async copy must outlive it
-    HC_CUDA(h, cudaStreamSynchronize(h->stream));
-  }
   return HC_OK;
 }
 
@@ -719,15 +774,17 @@ bool graph_eligible(hc_handle* h) {
   return true;
 }
 
+// Captures `steps` (1 or 2) steps starting on buffer parity `parity` into
+// h->graph (two steps, the parity returns) or h->graph1 (one step).
 template <typename T>
-int build_graph(hc_handle* h, int parity) {
+int build_graph(hc_handle* h, int parity, int steps = 2) {
   const int save_cur = h->cur, save_iter = h->iter;
   const bool save_sd = h->spread_done, save_sa = h->stamp_ahead;
   h->cur = parity;
   cudaGraph_t g = nullptr;
   HC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   int rc = enq_step<T>(h);
-  if (rc == HC_OK) rc = enq_step<T>(h);
+  if (rc == HC_OK && steps == 2) rc = enq_step<T>(h);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   h->cur = save_cur;
   h->iter = save_iter;
@@ -738,7 +795,7 @@ int build_graph(hc_handle* h, int parity) {
     return rc;
   }
   if (e != cudaSuccess) return fail(h, HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&h->graph[parity], g, 0);
+  e = cudaGraphInstantiate(steps == 2 ? &h->graph[parity] : &h->graph1[parity], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(h, HC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return HC_OK;
@@ -763,6 +820,16 @@ int run_steps(hc_handle* h, int nsteps) {
       h->iter += 2;
       nsteps -= 2;
     }
+  }
+  // a single step in the same state (iterate(1) in a loop) replays the
+  // one-step graph of its parity; the step flips the buffers
+  // (invalidate_graph, run on every state change, drops these graphs too)
+  if (nsteps == 1 && graph_eligible(h) && (!fusable(h) || h->spread_done)) {
+    if (!h->graph1[h->cur] && (rc = build_graph<T>(h, h->cur, 1)) != HC_OK) return rc;
+    HC_CUDA(h, cudaGraphLaunch(h->graph1[h->cur], h->stream));
+    h->iter += 1;
+    h->cur ^= 1;
+    return HC_OK;
   }
   for (int k = 0; k < nsteps; ++k)
     if ((rc = enq_step<T>(h)) != HC_OK) return rc;
@@ -1339,6 +1406,19 @@ int hc_destroy(hc_handle* h) {
                   h->frep_cell, h->frep_wall, h->fluid};
   for (void* q : ptrs) dfree(h, q);
   for (auto e : h->prof_ev) cudaEventDestroy(e);
+  if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
+  for (int k = 0; k < 2; ++k) {
+    dfree(h, h->pos_stage[k]);
+    if (h->pos_ready[k]) cudaEventDestroy(h->pos_ready[k]);
+    if (h->pos_copied[k]) cudaEventDestroy(h->pos_copied[k]);
+  }
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+  dfree(h, h->bodyd);
+  if (h->body_copied) {
+    cudaEventSynchronize(h->body_copied);
+    cudaEventDestroy(h->body_copied);
+  }
+  if (h->hbody_pin) cudaFreeHost(h->hbody_pin);
   if (h->pool) release_pool(h->p.device, h->stream);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -1382,13 +1462,35 @@ int hc_set_body_force(hc_handle* h, int mode, const double* p) {
   if (!h) return HC_ERR_INVALID;
   if (mode < HC_BODY_NONE || mode > HC_BODY_KOLMOGOROV) return fail(h, HC_ERR_INVALID, "unknown body-force mode");
   if (mode != HC_BODY_NONE && !p) return fail(h, HC_ERR_INVALID, "body-force parameters missing");
-  // the driver's setExternalVector after every iterate(): the same force again
-  // changes nothing (the reset to it is part of the collide-stream)
+  // the driver's setExternalVector after every iterate(): the profile is
+  // copied again, and the same force changes nothing else (the reset to it is
+  // part of the collide-stream)
   if (mode == h->body_mode &&
       (mode == HC_BODY_NONE || (p[0] == h->body[0] && (mode == HC_BODY_KOLMOGOROV || (p[1] == h->body[1] && p[2] == h->body[2])))))
+    return upload_profile(h, body_profile(h), nullptr);
+  if (h->spread_done) {
+    // the next step's force field holds the old body force and the spread
+    // fused into it: add the change of the body force, keep the spread
+    const std::vector<double> old = body_profile(h);
+    h->body_mode = mode;
+    for (int a = 0; a < 3; ++a) h->body[a] = (mode != HC_BODY_NONE) ? p[a] : 0.0;
+    if (mode == HC_BODY_KOLMOGOROV) h->body[1] = h->body[2] = 0.0;
+    const std::vector<double> prof = body_profile(h);
+    std::vector<double> change(prof.size());
+    for (size_t k = 0; k < prof.size(); ++k) change[k] = prof[k] - old[k];
+    int rc;
+    if ((rc = upload_profile(h, prof, &change)) != HC_OK) return rc;
+    const long long plane = (long long)h->nx * h->ny;
+    if (h->f64)
+      HC_CUDA(h, hcd::launch_add_body<double>((double*)h->F[h->cur], (const double*)h->bodyd, plane, h->nz, h->N,
+                                              h->stream));
+    else
+      HC_CUDA(h, hcd::launch_add_body<float>((float*)h->F[h->cur], (const float*)h->bodyd, plane, h->nz, h->N,
+                                             h->stream));
     return HC_OK;
-  // the force field is refilled with the body force: a spread already fused
-  // into it is dropped (and the node-tag stamp caught up) first
+  }
+  // the force field is refilled with the body force (the node-tag stamp
+  // caught up with a fused advance first)
   int rc0 = undo_fused_spread(h);
   if (rc0 != HC_OK) return rc0;
   h->body_mode = mode;
@@ -1777,6 +1879,48 @@ int hc_read_vertices(hc_handle* h, double* x, double* v, double* f) {
   return HC_OK;
 }
 
+int hc_read_positions_async(hc_handle* h, double* x, int slot) {
+  if (!h || !x || slot < 0 || slot > 1) return HC_ERR_INVALID;
+  if (h->nvert == 0) return HC_OK;
+  if (!h->copy_stream) {
+    HC_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      HC_CUDA(h, cudaEventCreateWithFlags(&h->pos_ready[k], cudaEventDisableTiming));
+      HC_CUDA(h, cudaEventCreateWithFlags(&h->pos_copied[k], cudaEventDisableTiming));
+    }
+  }
+  if (h->pos_stage_v < h->nvert) {
+    // new staging buffers once the copies out of the old ones are done
+    HC_CUDA(h, cudaStreamSynchronize(h->copy_stream));
+    for (int k = 0; k < 2; ++k) {
+      dfree(h, h->pos_stage[k]);
+      h->pos_stage[k] = nullptr;
+      if (h->pos_stage_v > 0) h->device_bytes -= 24 * h->pos_stage_v;
+    }
+    h->pos_stage_v = 0;
+    for (int k = 0; k < 2; ++k) HC_CUDA(h, dalloc(h, (void**)&h->pos_stage[k], 24 * (size_t)h->Vcap));
+    h->pos_stage_v = h->Vcap;
+    h->pos_inflight[0] = h->pos_inflight[1] = false;
+  }
+  // the staging buffer is rewritten only after its last copy left it
+  if (h->pos_inflight[slot]) HC_CUDA(h, cudaStreamWaitEvent(h->stream, h->pos_copied[slot], 0));
+  HC_CUDA(h, hcd::launch_soa_to_aos<double>(h->x, h->pos_stage[slot], h->Vcap, h->nvert, h->stream));
+  HC_CUDA(h, cudaEventRecord(h->pos_ready[slot], h->stream));
+  HC_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->pos_ready[slot], 0));
+  HC_CUDA(h, cudaMemcpyAsync(x, h->pos_stage[slot], 24 * (size_t)h->nvert, cudaMemcpyDeviceToHost, h->copy_stream));
+  HC_CUDA(h, cudaEventRecord(h->pos_copied[slot], h->copy_stream));
+  h->pos_inflight[slot] = true;
+  return HC_OK;
+}
+
+int hc_wait_positions(hc_handle* h, int slot) {
+  if (!h || slot < 0 || slot > 1) return HC_ERR_INVALID;
+  if (!h->pos_inflight[slot]) return HC_OK;
+  h->pos_inflight[slot] = false;
+  HC_CUDA(h, cudaEventSynchronize(h->pos_copied[slot]));
+  return HC_OK;
+}
+
 int hc_write_vertices(hc_handle* h, const double* x, const double* v, const double* f) {
   if (!h) return HC_ERR_INVALID;
   if (int rc0 = undo_fused_spread(h)) return rc0;
@@ -1891,6 +2035,8 @@ int hc_get_stats(hc_handle* h, hc_stats* out) {
   out->cells_alive = alive;
   return HC_OK;
 }
+
+int hc_vertex_count(const hc_handle* h) { return h ? h->nvert : HC_ERR_INVALID; }
 
 int hc_device_status(hc_handle* h, unsigned int* status) {
   if (!h || !status) return HC_ERR_INVALID;

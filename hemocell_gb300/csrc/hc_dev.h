@@ -230,6 +230,9 @@ cudaError_t launch_field_in(const double* in, T* F, long long N, cudaStream_t s)
 template <typename T>
 cudaError_t launch_fill_body(T* F, const T* bodyz, long long plane, int nz, long long N, cudaStream_t s);
 template <typename T>
+cudaError_t launch_add_body(T* F, const T* dz, long long plane, int nz, long long N, cudaStream_t s);
+cudaError_t launch_copy_words(void* dst, const void* src, size_t bytes, cudaStream_t s);
+template <typename T>
 size_t field_bytes(long long N);
 template <typename T>
 cudaError_t launch_convert_in(const double* src, T* dst, long long n, cudaStream_t s);

@@ -645,6 +645,36 @@ __global__ void k_fill_body(T* F, const T* bodyz, long long plane, int nz, long 
   const int z = (int)(n / plane);
   FieldLayout<T>::store(F, N, n, bodyz[z], bodyz[nz + z], bodyz[2 * nz + z]);
 }
+// Copy of n 32-bit words from mapped pinned host memory into device memory
+// by a kernel: a small per-step upload that does not wait behind a large
+// device-to-host transfer on a copy engine.
+__global__ void k_copy_words(uint32_t* dst, const uint32_t* src, int n) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) dst[k] = src[k];
+}
+cudaError_t launch_copy_words(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  const int n = (int)(bytes / 4);
+  if (n <= 0) return cudaSuccess;
+  k_copy_words<<<std::min((n + 255) / 256, 64), 256, 0, s>>>(static_cast<uint32_t*>(dst),
+                                                             static_cast<const uint32_t*>(src), n);
+  return cudaGetLastError();
+}
+
+// A changed body force applied to a force field that already holds the old
+// one (and possibly the next step's spread): F += delta of its plane.
+template <typename T>
+__global__ void k_add_body(T* F, const T* dz, long long plane, int nz, long long N) {
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int z = (int)(n / plane);
+  T x, y, w;
+  FieldLayout<T>::load(F, N, n, x, y, w);
+  FieldLayout<T>::store(F, N, n, x + dz[z], y + dz[nz + z], w + dz[2 * nz + z]);
+}
+template <typename T>
+cudaError_t launch_add_body(T* F, const T* dz, long long plane, int nz, long long N, cudaStream_t s) {
+  k_add_body<T><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(F, dz, plane, nz, N);
+  return cudaGetLastError();
+}
 template <typename T>
 cudaError_t launch_field_out(const T* F, double* out, long long N, cudaStream_t s) {
   k_field_out<T><<<(unsigned)((N + 255) / 256), 256, 0, s>>>(F, out, N);
@@ -693,6 +723,7 @@ cudaError_t launch_bump_stamp(uint32_t* stamp, cudaStream_t s) {
   template cudaError_t launch_node_velocity_fluid<T>(const LbmView<T>&, cudaStream_t);                   \
   template cudaError_t launch_node_velocity_packed<T>(const LbmView<T>&, cudaStream_t);                  \
   template cudaError_t launch_collide_stream_fluid<T>(const LbmView<T>&, int, cudaStream_t);             \
+  template cudaError_t launch_add_body<T>(T*, const T*, long long, int, long long, cudaStream_t);             \
   template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);             \
   template cudaError_t launch_stream_out<T>(const LbmView<T>&, double*, cudaStream_t);                   \
   template cudaError_t launch_stream_in<T>(const LbmView<T>&, const double*, double, const double*,       \

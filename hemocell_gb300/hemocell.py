@@ -171,6 +171,7 @@ class HemoCell:
         self.form = form
         self.types: list[Mesh] = []
         self.cell_types: list[int] = []
+        self._pending: dict[int, np.ndarray] = {}
 
     # --- lifecycle
     def close(self):
@@ -304,6 +305,25 @@ class HemoCell:
             out = np.zeros((self.stats().vertices, 3))
         self._check(self._lib.hc_read_vertices(self._h, _dp(out), None, None))
         return out
+
+    def read_positions_async(self, out: np.ndarray, slot: int = 0) -> None:
+        """Start copying the positions (after the steps queued so far) into a
+        caller-owned C-contiguous (V,3) float64 buffer in pinned host memory,
+        without waiting; the copy runs on its own stream while later steps
+        compute.  ``out`` must stay alive and untouched until
+        ``wait_positions(slot)``; two slots allow double buffering."""
+        nv = self._lib.hc_vertex_count(self._h)   # stats() would wait for the stream
+        if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.shape != (nv, 3):
+            raise HemoCellError("read_positions_async needs a C-contiguous (V,3) float64 buffer")
+        if not hasattr(self, "_pending"):
+            self._pending = {}
+        self._pending[slot] = out
+        self._check(self._lib.hc_read_positions_async(self._h, _dp(out), slot))
+
+    def wait_positions(self, slot: int = 0) -> np.ndarray:
+        """Wait for the copy started by read_positions_async(slot); returns its buffer."""
+        self._check(self._lib.hc_wait_positions(self._h, slot))
+        return getattr(self, "_pending", {}).pop(slot, None)
 
     # --- readback
     def read_fluid(self):

@@ -104,6 +104,10 @@ int hc_derived_units(const hc_handle* h, double* out6);
  * examples/pipeflow/pipeflow.cpp:141-146, lattice.initialize()) */
 int hc_set_flags(hc_handle* h, const uint8_t* flags); /* per node: 0 fluid, k>0 wall class k */
 int hc_set_wall_velocity(hc_handle* h, int cls, const double* u3);
+/* setExternalVector: the per-plane profile (3 x nz values of the form's
+ * type) is copied to the device from a pinned staging buffer on every call;
+ * the same force again changes nothing else, a changed one is added to the
+ * next step's force field (which keeps a spread already fused into it) */
 int hc_set_body_force(hc_handle* h, int mode, const double* p);
 int hc_init_equilibrium(hc_handle* h, double rho, const double* u3);
 
@@ -170,6 +174,13 @@ int hc_read_force_field(hc_handle* h, double* F, int which);   /* 0 next, 1 last
 int hc_write_force_field(hc_handle* h, const double* F);       /* sets the next force field */
 int hc_read_vertices(hc_handle* h, double* x, double* v, double* f); /* [V][3] each, may be NULL */
 int hc_write_vertices(hc_handle* h, const double* x, const double* v, const double* f);
+/* positions [V][3] copied to the host after the work queued so far, without
+ * waiting: a kernel gathers them into device staging buffer `slot` (0 or 1)
+ * on the handle's stream and a copy stream moves them into x (pinned host
+ * memory, untouched until hc_wait_positions(slot) returns), so the next
+ * steps run during the copy; a slot is reused only after its last copy */
+int hc_read_positions_async(hc_handle* h, double* x, int slot);
+int hc_wait_positions(hc_handle* h, int slot);
 int hc_read_cells(hc_handle* h, int* alive, double* volume);
 /* update_pg / ownership / neighbour lists (core/hemoCellParticleField.cpp:137-168):
  * vertex_node[V], vertex_tile[V], tile_offsets[ntiles+1], tile_vertices[V],
@@ -231,7 +242,8 @@ int hc_save_checkpoint(hc_handle* h, const char* dir);
  * created with the same lattice size, form and cell types; a handle without
  * cells receives the checkpoint's cells, one with cells must hold the same */
 int hc_load_checkpoint(hc_handle* h, const char* dir);
-int hc_get_stats(hc_handle* h, hc_stats* out);
+int hc_get_stats(hc_handle* h, hc_stats* out);  /* waits for the handle's stream (alive cells) */
+int hc_vertex_count(const hc_handle* h);         /* vertices in use; does not wait */
 /* device status word, sticky: bit0 non-finite vertex velocity, bit1 cell
  * deleted at a wall, bit2 a shared-memory pipeline wait of the bulk-copy
  * collide-stream timed out (the step's results are then invalid), bit3 a
