@@ -43,9 +43,11 @@ sys.path.insert(0, ROOT)
 BYTES_NODE = {"f32": 2 * 19 * 4 + 2 * 3 * 4, "f64": 2 * 19 * 8 + 2 * 3 * 8}
 BYTES_VERTEX = {"f32": 2 * 3 * 8 + 2 * 2 * 3 * 4, "f64": 2 * 3 * 3 * 8}
 # DRAM bytes of one collide-stream launch on this workload, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum, --set full capture of the
-# 64x64x256 pipe with 279 RBC; the summary is in profiles/)
-K1_TRAFFIC_PER_LAUNCH = {"f32": 105.014784e6 + 33.601536e6, "f64": 174.845696e6 + 93.809152e6}
+# (dram__bytes_read.sum + dram__bytes_write.sum of the 64x64x256 pipe with 279
+# RBC): FP32 inside graph-replayed steps (one pass, caches as the previous
+# kernel left them, mean of 4 launches), FP64 from a --set full capture of the
+# tuned FP64 kernel; the summaries are in profiles/
+K1_TRAFFIC_PER_LAUNCH = {"f32": 82.571584e6 + 64.570048e6, "f64": 178.035456e6 + 89.346560e6}
 
 
 def cpu_model() -> str:
@@ -254,11 +256,17 @@ def kolmogorov_leg(steps: int, warmup: int, tune_cache):
     out = {"workload": "kolmogorov_128: 128^3 periodic, F_x = A sin(2 pi z/128), 30% RBC (642 vertices), "
                        "PLT (162 vertices) 1 per 10 RBC, 2 WBC (2562 vertices)",
            "cells": len(case.cells), "vertices": case.nvertices, "packing_s": pack_s}
+    peak, _ = measured_peaks()
     for name, form in (("fp32_batched", L.HC_FORM_MIXED_F32), ("fp64_batched", L.HC_FORM_PLAIN_F64)):
         ms, prof, clocks, st, status, tuning = time_form(case, form, L.HC_LAUNCH_BATCHED, steps, warmup,
                                                          tune_cache)
         out[name] = {"value": case.N * steps / (ms * 1e3), "unit": "MLUPS", "ms_per_step": ms / steps,
                      "kernels_ms": prof, "tuning": tuning, "status": status, "clocks": clocks}
+        # the collide-stream on a lattice without walls (every node fluid)
+        k1_bytes = case.N * BYTES_NODE["f32" if form == L.HC_FORM_MIXED_F32 else "f64"]
+        gbs = k1_bytes / (prof["collide_stream"] * 1e-3) / 1e9
+        out[name]["collide_stream_roofline"] = {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                                                "algorithmic_bytes_per_launch": k1_bytes}
     out["fp32_over_fp64"] = out["fp32_batched"]["value"] / out["fp64_batched"]["value"]
     out["_case"] = case
     return out
