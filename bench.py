@@ -448,8 +448,14 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "kernel": "k_collide_stream<float>",
                          "peak_source": peak_kind, "algorithmic_bytes_per_launch": k1_bytes,
-                         "launch_ms": k1_ms},
-            "step_roofline": {"bytes_per_step": step_bytes, "achieved_gbs": step_gbs, "frac": step_gbs / peak},
+                         "launch_ms": k1_ms,
+                         # the same with every lattice node counted (the wall nodes' populations
+                         # are neither read nor written here, so this credits bytes not moved)
+                         "frac_all_nodes": case.N * BYTES_NODE["f32"] / (k1_ms * 1e-3) / 1e9 / peak},
+            "step_roofline": {"bytes_per_step": step_bytes, "achieved_gbs": step_gbs, "frac": step_gbs / peak,
+                              # N (all nodes) x 176 B + V x 72 B per step
+                              "frac_all_nodes": (case.N * BYTES_NODE["f32"] + st.vertices * 72) /
+                                                (ms / args.steps * 1e-3) / 1e9 / peak},
             "kernels_ms": prof,
             "clocks": clocks,
             "e2e": {"value": e2e_val, "unit": "MLUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -10,6 +10,7 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <numeric>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -120,6 +121,11 @@ struct hc_handle {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   // one-step graphs (iterate(1)), per buffer parity, built on first use
   cudaGraphExec_t graph1[2] = {nullptr, nullptr};
+  // with timescale separation: a graph of one whole cycle of cycle_len steps
+  // (the least common multiple of 2 and every timescale), captured starting
+  // at an iteration that is a multiple of it, per buffer parity there
+  cudaGraphExec_t cycle_graph[2] = {nullptr, nullptr};
+  int cycle_len = 0;
   bool graph_valid = false;
   long long device_bytes = 0;
   cudaMemPool_t pool = nullptr;  // this device's library pool (all allocations)
@@ -230,11 +236,16 @@ void dfree(hc_handle* h, void* p) {
 }
 
 void invalidate_graph(hc_handle* h) {
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < 2; ++k) {
     if (h->graph1[k]) {
       cudaGraphExecDestroy(h->graph1[k]);
       h->graph1[k] = nullptr;
     }
+    if (h->cycle_graph[k]) {
+      cudaGraphExecDestroy(h->cycle_graph[k]);
+      h->cycle_graph[k] = nullptr;
+    }
+  }
   for (int k = 0; k < 2; ++k)
     if (h->graph[k]) {
       cudaGraphExecDestroy(h->graph[k]);
@@ -774,8 +785,24 @@ bool graph_eligible(hc_handle* h) {
   return true;
 }
 
-// Captures `steps` (1 or 2) steps starting on buffer parity `parity` into
-// h->graph (two steps, the parity returns) or h->graph1 (one step).
+// Steps of one timescale cycle of the batched launch: the least common
+// multiple of 2 (the buffer parity) and every timescale in use, or 0 when
+// there is none to cycle (every timescale 1: the two-step graphs serve) or
+// the cycle exceeds 64 steps.
+int timescale_cycle(const hc_handle* h) {
+  if (h->p.launch != HC_LAUNCH_BATCHED) return 0;
+  long long L = 2;
+  auto lcm = [](long long a, long long b) { return a / std::gcd(a, b) * b; };
+  L = lcm(L, h->velocity_every);
+  for (const TypeSlot& ts : h->types) L = lcm(L, ts.every);
+  if (h->rep_every > 0) L = lcm(L, h->rep_every);
+  if (h->brep_every > 0) L = lcm(L, h->brep_every);
+  return (L > 2 && L <= 64) ? (int)L : 0;
+}
+
+// Captures `steps` steps starting on buffer parity `parity` into h->graph
+// (two steps, the parity returns), h->graph1 (one step) or h->cycle_graph
+// (a whole timescale cycle, starting at h->iter).
 template <typename T>
 int build_graph(hc_handle* h, int parity, int steps = 2) {
   const int save_cur = h->cur, save_iter = h->iter;
@@ -784,7 +811,7 @@ int build_graph(hc_handle* h, int parity, int steps = 2) {
   cudaGraph_t g = nullptr;
   HC_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   int rc = enq_step<T>(h);
-  if (rc == HC_OK && steps == 2) rc = enq_step<T>(h);
+  for (int k = 1; k < steps && rc == HC_OK; ++k) rc = enq_step<T>(h);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   h->cur = save_cur;
   h->iter = save_iter;
@@ -795,7 +822,8 @@ int build_graph(hc_handle* h, int parity, int steps = 2) {
     return rc;
   }
   if (e != cudaSuccess) return fail(h, HC_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(steps == 2 ? &h->graph[parity] : &h->graph1[parity], g, 0);
+  e = cudaGraphInstantiate(steps == 2 ? &h->graph[parity] : (steps == 1 ? &h->graph1[parity] : &h->cycle_graph[parity]),
+                           g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(h, HC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return HC_OK;
@@ -804,6 +832,25 @@ int build_graph(hc_handle* h, int parity, int steps = 2) {
 template <typename T>
 int run_steps(hc_handle* h, int nsteps) {
   int rc;
+  // timescale separation: eager steps up to the start of a cycle, then whole
+  // cycles replayed from their graph
+  const int L = timescale_cycle(h);
+  if (L > 0 && nsteps >= 2 * L) {
+    while (nsteps > 0 && (h->iter % L != 0 || (fusable(h) && !h->spread_done))) {
+      if ((rc = enq_step<T>(h)) != HC_OK) return rc;
+      nsteps--;
+    }
+    if (h->cycle_len != L) {
+      invalidate_graph(h);
+      h->cycle_len = L;
+    }
+    while (nsteps >= L) {
+      if (!h->cycle_graph[h->cur] && (rc = build_graph<T>(h, h->cur, L)) != HC_OK) return rc;
+      HC_CUDA(h, cudaGraphLaunch(h->cycle_graph[h->cur], h->stream));
+      h->iter += L;
+      nsteps -= L;
+    }
+  }
   if (graph_eligible(h) && nsteps >= 3 && fusable(h) && !h->spread_done) {
     if ((rc = enq_step<T>(h)) != HC_OK) return rc;  // leaves the next spread done
     nsteps--;

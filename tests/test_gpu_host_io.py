@@ -107,3 +107,35 @@ def test_single_steps_match_one_call(built, form, launch):
     assert a.device_status() == b.device_status()
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_timescale_cycle_graph(built, form):
+    """Materials every 6, 3 and 6 steps, velocity every 3 (a 6-step cycle):
+    the batched launch replays whole cycles from one CUDA graph (after eager
+    steps up to a cycle start) and ends where single eager steps end, and the
+    FP64 form where the oracle ends."""
+    from hemocell_gb300 import _lib as L
+    from oracle import oracle as orc
+    case = _cases().mixed_box(wall=True)
+    a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    for hc in (a, b):
+        hc.iterate(1)
+        hc.setMaterialTimeScaleSeparation([6, 3, 6], velocity_every=3)
+    a.iterate(40)
+    for _ in range(40):
+        b.iterate(1)
+    # up to the order of the spread's atomic additions (FP32 rounding in the mixed form)
+    tol = 1e-14 if form == 0 else 1e-6
+    assert rel_l2(a.read_vertices()[0], b.read_vertices()[0]) <= tol
+    assert rel_l2(a.read_fluid()[1], b.read_fluid()[1]) <= tol
+    assert a.stats().iter == b.stats().iter == 41
+    if form == 0:
+        o = orc.apply_case(case)
+        o.step(1)
+        o.set_timescales([6, 3, 6], 3)
+        o.step(40)
+        assert rel_l2(a.read_vertices()[0], o.read_vertices()[0]) < 1e-10
+    a.close()
+    b.close()
