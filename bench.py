@@ -47,6 +47,7 @@ BYTES_VERTEX = {"f32": 2 * 3 * 8 + 2 * 2 * 3 * 4, "f64": 2 * 3 * 3 * 8}
 # RBC): FP32 inside graph-replayed steps (one pass, caches as the previous
 # kernel left them, mean of 4 launches), FP64 from a --set full capture of the
 # tuned FP64 kernel; the summaries are in profiles/
+PIPE_WORKLOAD = "pipe_ht25 64x64x256 D3Q19, R=30 cylinder, 279 RBC (642 vertices), 25% Ht"
 K1_TRAFFIC_PER_LAUNCH = {"f32": 82.571584e6 + 64.570048e6, "f64": 178.035456e6 + 89.346560e6}
 
 
@@ -272,6 +273,25 @@ def kolmogorov_leg(steps: int, warmup: int, tune_cache):
     return out
 
 
+def timescale_leg(steps: int, warmup: int):
+    """The pipe with the RBC mechanics every 20 steps and the velocity update
+    every step (stepMaterialEvery = 20 of the reference's performance-testing
+    configurations): FP32 batched, whole 20-step cycles replayed as one graph."""
+    from hemocell_gb300 import _lib as L
+    from hemocell_gb300 import cases
+    case = cases.pipe_ht25(seed=1)
+    hc = case.build(form=L.HC_FORM_MIXED_F32, launch=L.HC_LAUNCH_BATCHED)
+    hc.setMaterialTimeScaleSeparation([20], velocity_every=1)
+    hc.iterate(max(warmup, 40))
+    hc.sync()
+    n = max(40, steps // 20 * 20)
+    ms = hc.time_steps(n)
+    status = hc.device_status()
+    hc.close()
+    return {"workload": "pipe_ht25 64x64x256, 279 RBC, RBC mechanics every 20 steps", "steps": n,
+            "value": case.N * n / (ms * 1e3), "unit": "MLUPS", "ms_per_step": ms / n, "status": status}
+
+
 def serving_leg(args):
     """Continuous batching of the stream of independent sheared-box solves
     (box edge 32-96, 1-8 RBC, 500-5000 steps, Poisson arrivals at 200/s):
@@ -335,7 +355,7 @@ def run_reference(args):
         "impl": "reference", "metric": "MLUPS incl. IBM+cell forces", "value": mlups, "unit": "MLUPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / n * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "pipe_ht25 64x64x256, 279 RBC (642 vertices), 25% Ht", "nodes": case.N,
+        "config": {"workload": PIPE_WORKLOAD, "nodes": case.N,
                    "vertices": case.nvertices, "form": "FP64 CPU restatement (oracle port)"},
         "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": f"{n} full steps of the workload (of {args.steps} requested) after "
@@ -411,6 +431,7 @@ def main():
 
     if not args.no_mixed_error:
         extra["mixed_vs_fp64"] = mixed_error_leg(case)
+    extra["materials_every_20"] = timescale_leg(min(args.steps, 2000), args.warmup)
     if not args.no_kolmogorov:
         extra["kolmogorov"] = kolmogorov_leg(min(args.steps, 1000), args.warmup, tune_cache)
     if not args.no_serving:
@@ -439,7 +460,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": "pipe_ht25 64x64x256 D3Q19, R=30 cylinder, 279 RBC (642 vertices), 25% Ht",
+            "config": {"workload": PIPE_WORKLOAD,
                        "form": "mixed FP32 populations f_i-w_i / FP64 positions+volume, batched + CUDA graph",
                        "nodes": case.N, "fluid_nodes": fluid, "vertices": st.vertices, "cells": st.cells,
                        "parallelism": "replicas" if world > 1 else "single",
