@@ -604,6 +604,7 @@ cudaError_t launch_k1(hc_handle* h, const LbmView<T>& L) {
 
 template <typename T>
 cudaError_t launch_nv(hc_handle* h, const LbmView<T>& L) {
+  if ((h->tune[7] & 0x300) == 0x300 && L.fast) return hcd::launch_node_velocity_dense<T>(L, h->stream);
   if ((h->tune[7] & 0x200) && L.fast) return hcd::launch_node_velocity_packed<T>(L, h->stream);
   if ((h->tune[7] & 0x100) && L.fluid) return hcd::launch_node_velocity_fluid<T>(L, h->stream);
   return hcd::launch_node_velocity<T>(L, h->stream);
@@ -1185,10 +1186,10 @@ int autotune(hc_handle* h, const char* cache) {
     // node velocity variant and the IBM block size
     best = 1e30f;
     int bb = h->tune[3], nvf = nvflags;
-    for (int fl : {0, 0x100, 0x200})
+    for (int fl : {0, 0x100, 0x200, 0x300})
       for (int bs : {64, 128, 256}) {
         if (fl == 0x100 && h->nfluid == 0) continue;
-        if (fl == 0x200 && 19LL * h->N >= (1LL << 31)) continue;
+        if (fl >= 0x200 && 19LL * h->N >= (1LL << 31)) continue;
         h->tune[2] = h->tune[3] = bs;
         h->tune[7] = b7 | fl;
         const float t = trial();
@@ -2121,10 +2122,11 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
   {
     const int mode = in8[7] & 0xff;
     if ((in8[7] & ~0x3fff) != 0) return fail(h, HC_ERR_INVALID, "tune[7]: only bits 0-13 are defined");
-    if ((in8[7] & 0x300) == 0x300) return fail(h, HC_ERR_INVALID, "tune[7]: one node-velocity variant at a time");
+    if ((in8[7] & 0x300) == 0x300 && 19LL * h->N >= (1LL << 31))
+      return fail(h, HC_ERR_INVALID, "tune[7]: the dense node velocity needs 19 N < 2^31");
     if ((in8[7] & 0x200) && 19LL * h->N >= (1LL << 31))
       return fail(h, HC_ERR_INVALID, "packed node velocity needs 19 N < 2^31");
-    if ((mode == 1 || (in8[7] & 0x100)) && h->nfluid == 0)
+    if ((mode == 1 || (in8[7] & 0x300) == 0x100) && h->nfluid == 0)
       return fail(h, HC_ERR_INVALID, "no fluid-node list for this lattice");
     if (mode >= 2) {
       const int st = mode & 15, ctas = mode >> 4;

@@ -216,6 +216,8 @@ template <typename T>
 cudaError_t launch_node_velocity_fluid(const LbmView<T>& L, cudaStream_t s);
 // tagged nodes packed into whole warps (needs L.fast)
 template <typename T>
+cudaError_t launch_node_velocity_dense(const LbmView<T>& L, cudaStream_t s);
+template <typename T>
 cudaError_t launch_node_velocity_packed(const LbmView<T>& L, cudaStream_t s);
 template <typename T>
 cudaError_t launch_moments(const LbmView<T>& L, double* rho, double* u, cudaStream_t s);

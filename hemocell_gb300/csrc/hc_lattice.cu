@@ -493,6 +493,40 @@ __global__ void __launch_bounds__(256) k_node_velocity_packed(const LbmView<T> L
   pdl_trigger();
 }
 
+// Node velocity at every fluid node, in the collide-stream's (x, y)-block
+// layout: whole warps of coalesced pulls, where the tagged forms pull only
+// the stencil nodes through partly used sectors.  Interpolation reads only
+// tagged nodes, whose values are the tagged forms' bits.  Needs 19 N < 2^31.
+template <typename T, bool MW>
+__global__ void __launch_bounds__(256) k_node_velocity_dense(const LbmView<T> L) {
+  pdl_wait();
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  const int Y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int Z = L.reverse ? L.nz - 1 - (int)blockIdx.z : (int)blockIdx.z;
+  if (X >= L.nx || Y >= L.ny) return;
+  const int n = X + L.nx * (Y + L.ny * Z);
+  const uint32_t m = __ldg(L.nbmask + n);
+  if (m & NB_SOLID) return;
+  T f[19];
+  if (m & NB_INTERIOR) pull_interior(L, L.fsrc, n, f);
+  else if (pull_is_inline(L, X, Y, Z, m)) pull_inline<T, MW>(L, L.fsrc, n, X, Y, Z, m, f);
+  else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
+  T rhoBar, jx, jy, jz, Fx, Fy, Fz;
+  moments(f, rhoBar, jx, jy, jz);
+  FieldLayout<T>::load(L.Fcur, L.N, n, Fx, Fy, Fz);
+  const T rho = T(1) + rhoBar;
+  FieldLayout<T>::store(L.unode, L.N, n, (jx + T(0.5) * Fx) / rho, (jy + T(0.5) * Fy) / rho,
+                        (jz + T(0.5) * Fz) / rho);
+  pdl_trigger();
+}
+
+template <typename T>
+cudaError_t launch_node_velocity_dense(const LbmView<T>& L, cudaStream_t s) {
+  const dim3 b(32, 8), g((L.nx + 31) / 32, (L.ny + 7) / 8, L.nz);
+  if (L.moving_walls) return launch_kernel(k_node_velocity_dense<T, true>, g, b, 0, s, L.pdl, L);
+  return launch_kernel(k_node_velocity_dense<T, false>, g, b, 0, s, L.pdl, L);
+}
+
 template <typename T>
 cudaError_t launch_node_velocity_packed(const LbmView<T>& L, cudaStream_t s) {
   const long long nchunks = (L.N + 255) / 256;
@@ -722,6 +756,7 @@ cudaError_t launch_bump_stamp(uint32_t* stamp, cudaStream_t s) {
   template cudaError_t launch_node_velocity<T>(const LbmView<T>&, cudaStream_t);                         \
   template cudaError_t launch_node_velocity_fluid<T>(const LbmView<T>&, cudaStream_t);                   \
   template cudaError_t launch_node_velocity_packed<T>(const LbmView<T>&, cudaStream_t);                  \
+  template cudaError_t launch_node_velocity_dense<T>(const LbmView<T>&, cudaStream_t);                   \
   template cudaError_t launch_collide_stream_fluid<T>(const LbmView<T>&, int, cudaStream_t);             \
   template cudaError_t launch_add_body<T>(T*, const T*, long long, int, long long, cudaStream_t);             \
   template cudaError_t launch_moments<T>(const LbmView<T>&, double*, double*, cudaStream_t);             \

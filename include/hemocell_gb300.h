@@ -261,8 +261,9 @@ int hc_get_tuning(hc_handle* h, int* out8);
  * mechanics variant (0 vertex gather, 1 face/edge scatter, 2 staged face/edge
  * terms gathered per vertex), and in8[7]: bits 0-7 the collide-stream kind
  * (0 (x,y)-blocks or rows, 1 one thread per fluid node, else bulk copies:
- * stages | CTAs per SM << 4), bit 8 node velocity per fluid node, bit 9 node
- * velocity over warp-packed tagged nodes, bit 10 programmatic dependent launch
+ * stages | CTAs per SM << 4), bits 8-9 the node velocity (0 every tagged node,
+ * 1 per fluid node, 2 over warp-packed tagged nodes, 3 every fluid node in
+ * whole coalesced warps), bit 10 programmatic dependent launch
  * of the step's kernels, bit 11 keeps interpolation + advance a kernel of
  * their own in the batched step (by default the force assembly does them),
  * and variants of the direct (x,y)-block and fluid-node collide-stream:
