@@ -48,7 +48,7 @@ BYTES_VERTEX = {"f32": 2 * 3 * 8 + 2 * 2 * 3 * 4, "f64": 2 * 3 * 3 * 8}
 # kernel left them, mean of 4 launches), FP64 from a --set full capture of the
 # tuned FP64 kernel; the summaries are in profiles/
 PIPE_WORKLOAD = "pipe_ht25 64x64x256 D3Q19, R=30 cylinder, 279 RBC (642 vertices), 25% Ht"
-K1_TRAFFIC_PER_LAUNCH = {"f32": 82.571584e6 + 64.570048e6, "f64": 178.035456e6 + 89.346560e6}
+K1_TRAFFIC_PER_LAUNCH = {"f32": 84.17e6 + 67.79e6, "f64": 178.035456e6 + 89.346560e6}
 
 
 def cpu_model() -> str:
