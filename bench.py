@@ -393,8 +393,15 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
+    from hemocell_gb300 import hemocell as _hc
+    _hc.set_default_device(local)   # every handle and batch of this rank on its own GPU
 
     import __graft_entry__ as g
+    if world > 1:
+        # one rank compiles; the others find the objects up to date
+        if rank == 0:
+            g.build()
+        torch.distributed.barrier()
     g.build()
     from hemocell_gb300 import _lib as L
     case = build_case(args.steps)

@@ -68,7 +68,7 @@ class Case:
     def flags_array(self) -> np.ndarray:
         return np.zeros(self.N, np.uint8) if self.flags is None else self.flags
 
-    def build(self, form: int = L.HC_FORM_PLAIN_F64, launch: int = L.HC_LAUNCH_PER_STAGE, device: int = 0,
+    def build(self, form: int = L.HC_FORM_PLAIN_F64, launch: int = L.HC_LAUNCH_PER_STAGE, device=None,
               tile=(8, 8, 8)) -> HemoCell:
         hc = HemoCell(*self.dims, periodic=self.periodic, dx=DX, dt=DT, rho_p=RHO_P, kBT_p=KBT, tau=self.tau,
                       form=form, launch=launch, device=device, tile=tile)

@@ -146,12 +146,26 @@ def pack_cells(dims, periodic, solid: Optional[np.ndarray], meshes: Sequence[Mes
     return centres[:n].copy(), angles[:n].copy(), types[:n].copy()
 
 
+_default_device = 0
+
+
+def set_default_device(device: int) -> None:
+    """The CUDA device of handles and batches created without an explicit one
+    (one process per GPU: its local rank)."""
+    global _default_device
+    _default_device = int(device)
+
+
+def default_device() -> int:
+    return _default_device
+
+
 class HemoCell:
     """One GB300-resident HemoCell instance (a D3Q19 lattice with its cells)."""
 
     def __init__(self, nx: int, ny: int, nz: int, periodic=(1, 1, 1), dx: float = 0.5e-6, dt: float = 1e-7,
                  nu_p: float = 0.0, rho_p: float = 1025.0, kBT_p: float = 4.100531391e-21, tau: float = 1.0,
-                 form: int = L.HC_FORM_PLAIN_F64, launch: int = L.HC_LAUNCH_PER_STAGE, device: int = 0,
+                 form: int = L.HC_FORM_PLAIN_F64, launch: int = L.HC_LAUNCH_PER_STAGE, device: Optional[int] = None,
                  tile=(8, 8, 8)):
         p = L.hc_params()
         p.nx, p.ny, p.nz = nx, ny, nz
@@ -159,7 +173,7 @@ class HemoCell:
             p.periodic[a] = int(periodic[a])
             p.tile[a] = int(tile[a])
         p.dx, p.dt, p.nu_p, p.rho_p, p.kBT_p, p.tau = dx, dt, nu_p, rho_p, kBT_p, tau
-        p.form, p.launch, p.device = form, launch, device
+        p.form, p.launch, p.device = form, launch, _default_device if device is None else device
         self._lib = L.lib()
         h = self._lib.hc_create(C.byref(p))
         if not h:
@@ -465,9 +479,10 @@ class Batch:
     ``read_*`` methods) and ``release`` frees it and its share of the budget.
     """
 
-    def __init__(self, budget_bytes: int, max_slots: int = 64, chunk_steps: int = 50, device: int = 0):
+    def __init__(self, budget_bytes: int, max_slots: int = 64, chunk_steps: int = 50, device: Optional[int] = None):
         self._lib = L.lib()
-        b = self._lib.hc_batch_create(device, int(budget_bytes), int(max_slots), int(chunk_steps))
+        dev = _default_device if device is None else device
+        b = self._lib.hc_batch_create(dev, int(budget_bytes), int(max_slots), int(chunk_steps))
         if not b:
             raise HemoCellError(self._lib.hc_last_error(None).decode())
         self._b = C.c_void_p(b)

@@ -25,9 +25,11 @@ def _rank(rank, world, port, q):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import bench
+    from hemocell_gb300 import hemocell
+    hemocell.set_default_device(rank)  # as bench.py does with LOCAL_RANK: each replica on its own GPU
     ms = 10.0 + 5.0 * rank            # rank 1 is the slower replica
     m = bench.max_over_ranks(ms)
-    q.put((rank, m, bench.replicas_mlups(world, 1_000_000, 100, m)))
+    q.put((rank, m, bench.replicas_mlups(world, 1_000_000, 100, m), hemocell.default_device()))
     dist.destroy_process_group()
 
 
@@ -45,6 +47,7 @@ def test_max_over_two_gloo_ranks():
     assert [g[1] for g in got] == [15.0, 15.0]
     # 2 replicas x 1e6 nodes x 100 steps in 15 ms
     assert got[0][2] == pytest.approx(2 * 1e6 * 100 / 15e3)
+    assert [g[3] for g in got] == [0, 1]
 
 
 def test_single_process_is_identity():
