@@ -72,11 +72,22 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def smi_id(local: int) -> str:
+    """nvidia-smi's id of CUDA device `local` of this process: its entry of
+    CUDA_VISIBLE_DEVICES (an index or a UUID) when that is set."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").strip()
+    if vis:
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        if local < len(ids):
+            return ids[local]
+    return str(local)
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
 
-    def __init__(self, index: int = 0):
-        self.index = index
+    def __init__(self, index=None):
+        self.index = smi_id(int(os.environ.get("LOCAL_RANK", "0"))) if index is None else index
         self.samples = []
         self.proc = None
 
