@@ -95,6 +95,7 @@ SIGNATURES = {
     "hc_read_positions_async": (C.c_int, [P, D, C.c_int]),
     "hc_wait_positions": (C.c_int, [P, C.c_int]),
     "hc_vertex_count": (C.c_int, [P]),
+    "hc_read_neighbours": (C.c_int, [P, I, I, C.c_int]),
     "hc_read_fluid": (C.c_int, [P, D, D]),
     "hc_read_populations": (C.c_int, [P, D]),
     "hc_write_populations": (C.c_int, [P, D]),

@@ -2037,6 +2037,42 @@ int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_off
   return nt;
 }
 
+int hc_read_neighbours(hc_handle* h, int* nb_offsets, int* nb_cells, int max_cells) {
+  if (!h || !nb_offsets || max_cells < 0 || (max_cells > 0 && !nb_cells)) return HC_ERR_INVALID;
+  int rc = hc_stage(h, HC_STAGE_BIN);
+  if (rc != HC_OK) return rc;
+  const int nt = h->ntiles;
+  const int per[3] = {h->p.periodic[0] ? 1 : 0, h->p.periodic[1] ? 1 : 0, h->p.periodic[2] ? 1 : 0};
+  // scratch: counts[nt], offsets[nt + 1], then the cells
+  const size_t head = 4 * (2 * (size_t)nt + 1);
+  if ((rc = ensure_scratch(h, head)) != HC_OK) return rc;
+  int* counts = reinterpret_cast<int*>(h->scratch);
+  int* offs = counts + nt;
+  HC_CUDA(h, hcd::launch_tile_neighbours(h->tg, per, h->tile_cell_offsets, h->tile_cells, nt, counts, nullptr,
+                                         nullptr, h->stream));
+  HC_CUDA(h, hcd::launch_exclusive_scan(counts, nt, offs, h->stream));
+  HC_CUDA(h, cudaMemcpyAsync(nb_offsets, offs, 4 * ((size_t)nt + 1), cudaMemcpyDeviceToHost, h->stream));
+  HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  const int total = nb_offsets[nt];
+  if (total > max_cells) {
+    shrink_scratch(h);
+    return fail(h, HC_ERR_INVALID, "nb_cells buffer too small");
+  }
+  if (total > 0) {
+    if ((rc = ensure_scratch(h, head + 4 * (size_t)total)) != HC_OK) return rc;
+    counts = reinterpret_cast<int*>(h->scratch);
+    offs = counts + nt;
+    int* cells = offs + nt + 1;
+    HC_CUDA(h, cudaMemcpyAsync(offs, nb_offsets, 4 * ((size_t)nt + 1), cudaMemcpyHostToDevice, h->stream));
+    HC_CUDA(h, hcd::launch_tile_neighbours(h->tg, per, h->tile_cell_offsets, h->tile_cells, nt, counts, offs, cells,
+                                           h->stream));
+    HC_CUDA(h, cudaMemcpyAsync(nb_cells, cells, 4 * (size_t)total, cudaMemcpyDeviceToHost, h->stream));
+    HC_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  shrink_scratch(h);
+  return nt;
+}
+
 long long hc_estimate_device_bytes(const hc_params* p, int nvertices, int ncells) {
   if (!p || p->nx <= 0 || p->ny <= 0 || p->nz <= 0 || nvertices < 0 || ncells < 0) return HC_ERR_INVALID;
   const long long N = (long long)p->nx * p->ny * p->nz;

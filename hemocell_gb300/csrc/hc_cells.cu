@@ -1628,6 +1628,73 @@ cudaError_t launch_exclusive_scan(const int* in, int n, int* out, cudaStream_t s
   return cudaGetLastError();
 }
 
+// Neighbour lists (the cells within the kernel halo of a tile): for tile t,
+// the distinct cells with vertices in t or in one of its 26 neighbouring
+// tiles (wrapped on periodic axes, cut at the others), ascending.  A 27-way
+// merge of the tiles' ascending cell lists (tile_cell_offsets / tile_cells);
+// `out` null counts only.
+__device__ int tile_neighbour_cells(const TileGrid tg, int per_x, int per_y, int per_z, const int* tco,
+                                    const int* tcells, int t, int* out) {
+  const int tx = t % tg.ntx, ty = (t / tg.ntx) % tg.nty, tz = t / (tg.ntx * tg.nty);
+  const int per[3] = {per_x, per_y, per_z};
+  const int n3[3] = {tg.ntx, tg.nty, tg.ntz};
+  int pos[27], end[27], tid[27], nl = 0;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        int c[3] = {tx + dx, ty + dy, tz + dz};
+        bool ok = true;
+        for (int a = 0; a < 3; ++a) {
+          if (c[a] < 0 || c[a] >= n3[a]) {
+            if (per[a]) c[a] = (c[a] + n3[a]) % n3[a];
+            else ok = false;
+          }
+        }
+        if (!ok) continue;
+        const int nt = c[0] + tg.ntx * (c[1] + tg.nty * c[2]);
+        bool dup = false;  // a small periodic grid wraps onto the same tile
+        for (int k = 0; k < nl; ++k)
+          if (tid[k] == nt) dup = true;
+        if (dup) continue;
+        tid[nl] = nt;
+        pos[nl] = tco[nt];
+        end[nl] = tco[nt + 1];
+        ++nl;
+      }
+  int count = 0, last = -1;
+  for (;;) {
+    int best = -1;
+    for (int k = 0; k < nl; ++k)
+      if (pos[k] < end[k] && (best < 0 || tcells[pos[k]] < best)) best = tcells[pos[k]];
+    if (best < 0) break;
+    for (int k = 0; k < nl; ++k)
+      while (pos[k] < end[k] && tcells[pos[k]] == best) ++pos[k];
+    if (best != last) {
+      if (out) out[count] = best;
+      ++count;
+      last = best;
+    }
+  }
+  return count;
+}
+
+__global__ void k_tile_neighbours(const TileGrid tg, int px, int py, int pz, const int* tco, const int* tcells,
+                                  int ntiles, int* counts, const int* offsets, int* cells) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  if (offsets) tile_neighbour_cells(tg, px, py, pz, tco, tcells, t, cells + offsets[t]);
+  else counts[t] = tile_neighbour_cells(tg, px, py, pz, tco, tcells, t, nullptr);
+}
+
+cudaError_t launch_tile_neighbours(const TileGrid& tg, const int per[3], const int* tile_cell_offsets,
+                                   const int* tile_cells, int ntiles, int* counts, const int* offsets, int* cells,
+                                   cudaStream_t s) {
+  if (ntiles <= 0) return cudaSuccess;
+  k_tile_neighbours<<<(ntiles + 127) / 128, 128, 0, s>>>(tg, per[0], per[1], per[2], tile_cell_offsets, tile_cells,
+                                                         ntiles, counts, offsets, cells);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* vcell, int ntiles,
                              int* tile_cell_counts, cudaStream_t s) {
   k_bin_sort<<<ntiles, 256, 0, s>>>(offsets, tile_vertices, vcell, tile_cell_counts);

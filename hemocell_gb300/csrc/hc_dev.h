@@ -275,6 +275,11 @@ cudaError_t launch_tile_cells(const int* offsets, const int* tile_vertices, cons
 // the two middle steps of the tile CSR on their own: out[0..n] = exclusive
 // scan of in[0..n-1]; per-tile sort of tile_vertices and distinct cells per tile
 cudaError_t launch_exclusive_scan(const int* in, int n, int* out, cudaStream_t s);
+// per tile, the ascending distinct cells of the tile and its 26 neighbours:
+// counts (offsets null) or the cells at offsets (counts unused)
+cudaError_t launch_tile_neighbours(const TileGrid& tg, const int per[3], const int* tile_cell_offsets,
+                                   const int* tile_cells, int ntiles, int* counts, const int* offsets, int* cells,
+                                   cudaStream_t s);
 cudaError_t launch_tile_sort(const int* offsets, int* tile_vertices, const int* vcell, int ntiles,
                              int* tile_cell_counts, cudaStream_t s);
 

@@ -423,6 +423,19 @@ class HemoCell:
         return dict(vertex_node=vn[:V], vertex_tile=vt[:V], tile_offsets=to[: nt + 1],
                     tile_vertices=tv[: to[nt]], tile_cell_offsets=tco[: nt + 1], tile_cells=tc[: tco[nt]])
 
+    def read_neighbours(self):
+        """Per tile, the sorted distinct cells of the tile and its 26
+        neighbouring tiles (the cells within the kernel halo), as CSR:
+        (offsets[ntiles + 1], cells)."""
+        b = self.read_bins()
+        nt = len(b["tile_cell_offsets"]) - 1
+        cap = max(27 * len(b["tile_cells"]), 1)
+        off = np.zeros(nt + 1, np.int32)
+        cells = np.zeros(cap, np.int32)
+        r = self._check(self._lib.hc_read_neighbours(self._h, _ip(off), _ip(cells), cap))
+        assert r == nt
+        return off, cells[: off[nt]].copy()
+
     def device_status(self) -> int:
         s = C.c_uint()
         self._check(self._lib.hc_device_status(self._h, C.byref(s)))

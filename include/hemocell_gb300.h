@@ -187,6 +187,12 @@ int hc_read_cells(hc_handle* h, int* alive, double* volume);
  * tile_cell_offsets[ntiles+1], tile_cells[max_tile_cells].  Returns ntiles. */
 int hc_read_bins(hc_handle* h, int* vertex_node, int* vertex_tile, int* tile_offsets,
                  int* tile_vertices, int* tile_cell_offsets, int* tile_cells, int max_tile_cells);
+/* Neighbour lists (block neighbours, core/hemoCellFields.cpp:230-236, on one
+ * lattice: the tiles within the kernel halo): for every tile, the ascending
+ * distinct cell ids with vertices in the tile or in one of its 26 neighbouring
+ * tiles, wrapped on periodic axes.  nb_offsets[ntiles+1] (CSR), nb_cells
+ * [max_cells].  Bins the current positions first.  Returns ntiles. */
+int hc_read_neighbours(hc_handle* h, int* nb_offsets, int* nb_cells, int max_cells);
 /* Tile binning that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that must not have a library allocate on
  * their behalf -- a program whose device memory is already carved up by its

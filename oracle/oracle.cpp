@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <set>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -1135,6 +1136,42 @@ int orc_bins(orc_sim* s, int tx, int ty, int tz, const double* xin, int* vertex_
   }
   tile_offsets[ntiles] = off;
   tile_cell_offsets[ntiles] = coff;
+  return ntiles;
+}
+
+// Neighbour lists: for each tile, the cells with vertices in it or in one of
+// its 26 neighbouring tiles (block neighbours core/hemoCellFields.cpp:230-236,
+// here tiles of one global lattice), wrapped on periodic axes, as sorted
+// distinct ids in CSR.  Input: the tile cell lists of orc_bins.
+int orc_neighbours(int ntx, int nty, int ntz, int px, int py, int pz, const int* tile_cell_offsets,
+                   const int* tile_cells, int* nb_offsets, int* nb_cells, int max_cells) {
+  const int n3[3] = {ntx, nty, ntz}, per[3] = {px, py, pz};
+  const int ntiles = ntx * nty * ntz;
+  int off = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const int c0[3] = {t % ntx, (t / ntx) % nty, t / (ntx * nty)};
+    std::set<int> tiles, cells;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          int c[3] = {c0[0] + dx, c0[1] + dy, c0[2] + dz};
+          bool ok = true;
+          for (int a = 0; a < 3; ++a)
+            if (c[a] < 0 || c[a] >= n3[a]) {
+              if (per[a]) c[a] = (c[a] + n3[a]) % n3[a];
+              else ok = false;
+            }
+          if (ok) tiles.insert(c[0] + ntx * (c[1] + nty * c[2]));
+        }
+    for (int u : tiles)
+      for (int k = tile_cell_offsets[u]; k < tile_cell_offsets[u + 1]; ++k) cells.insert(tile_cells[k]);
+    nb_offsets[t] = off;
+    for (int c : cells) {
+      if (off >= max_cells) return -1;
+      nb_cells[off++] = c;
+    }
+  }
+  nb_offsets[ntiles] = off;
   return ntiles;
 }
 

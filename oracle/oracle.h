@@ -98,6 +98,10 @@ int orc_bins(orc_sim* s, int tx, int ty, int tz, const double* x,
              int* vertex_node, int* vertex_tile, int* tile_offsets,
              int* tile_vertices, int* tile_cell_offsets, int* tile_cells,
              int max_tile_cells);
+/* neighbour lists from the tile cell lists of orc_bins: per tile, sorted
+ * distinct cells of the tile and its 26 neighbours (periodic axes wrapped) */
+int orc_neighbours(int ntx, int nty, int ntz, int px, int py, int pz, const int* tile_cell_offsets,
+                   const int* tile_cells, int* nb_offsets, int* nb_cells, int max_cells);
 
 /* CommonCellConstants export for tests: sizes (nE, nI) and arrays */
 int orc_type_sizes(orc_sim* s, int type, int* out4);

@@ -56,6 +56,7 @@ _SIG = {
     "orc_write_vertices": (None, [P, D, D, D]),
     "orc_read_cells": (None, [P, I, D]),
     "orc_bins": (C.c_int, [P, C.c_int, C.c_int, C.c_int, D, I, I, I, I, I, I, C.c_int]),
+    "orc_neighbours": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, I, I, I, I, C.c_int]),
     "orc_type_sizes": (C.c_int, [P, C.c_int, I]),
     "orc_type_constants": (None, [P, C.c_int, I, D, D, I, I, D, D, I, D]),
     "orc_units": (None, [C.c_double] * 6 + [D]),
@@ -232,6 +233,19 @@ class Oracle:
         assert r == nt
         return dict(vertex_node=vn[:V], vertex_tile=vt[:V], tile_offsets=to, tile_vertices=tv[: to[nt]],
                     tile_cell_offsets=tco, tile_cells=tc[: tco[nt]])
+
+    def neighbours(self, tile=(8, 8, 8), x=None, dims=None, periodic=(1, 1, 1)):
+        """Per tile, the sorted distinct cells of the tile and its 26 neighbours (CSR)."""
+        b = self.bins(tile, x, dims)
+        nt3 = [-(-dims[a] // tile[a]) for a in range(3)]
+        nt = nt3[0] * nt3[1] * nt3[2]
+        cap = max(27 * len(b["tile_cells"]), 1)
+        off, cells = np.zeros(nt + 1, np.int32), np.zeros(cap, np.int32)
+        tco = np.ascontiguousarray(b["tile_cell_offsets"], np.int32)
+        tc = np.ascontiguousarray(np.append(b["tile_cells"], 0), np.int32)
+        r = self.L.orc_neighbours(*nt3, *[int(p) for p in periodic], _i(tco), _i(tc), _i(off), _i(cells), cap)
+        assert r == nt
+        return off, cells[: off[nt]].copy()
 
     def type_constants(self, t):
         sz = np.zeros(4, np.int32)

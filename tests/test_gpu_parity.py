@@ -262,6 +262,34 @@ def test_advance_and_bins_bit_exact(built):
     hc.close()
 
 
+@pytest.mark.parametrize("which", ["walls", "periodic", "suspension"])
+def test_neighbour_lists_bit_exact(built, which):
+    """hc_read_neighbours (per tile, the cells of the tile and its 26
+    neighbours) against the oracle, on the same positions: bit-exact, with
+    non-periodic walls in z, fully periodic, and on a 36^3 suspension whose
+    4 x 4 x 4 tile grid wraps onto itself at the edges of 9-tile axes."""
+    C = _cases()
+    if which == "walls":
+        case, tile = mixed_box(wall=True), (8, 8, 8)
+    elif which == "periodic":
+        case, tile = mixed_box(wall=False), (4, 4, 4)
+    else:
+        case = C.kolmogorov_mix(n=36, rbc_fraction=0.15, n_wbc=1, plt_per_rbc=0.5, wbc_triangles=320, seed=5)
+        tile = (4, 4, 4)
+    from hemocell_gb300 import _lib as L
+    hc = case.build(tile=tile)
+    o = _orc().apply_case(case)
+    hc.iterate(5)
+    o.step(5)
+    xg, _, _ = hc.read_vertices()
+    off, cells = hc.read_neighbours()
+    off_o, cells_o = o.neighbours(tile, xg, case.dims, case.periodic)
+    assert np.array_equal(off, off_o)
+    assert np.array_equal(cells, cells_o)
+    assert len(cells) > 0 and np.all(np.diff(off) >= 0)
+    hc.close()
+
+
 @pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("types", [[0], [1], [2], [0, 1, 2]])
 def test_mechanics_stage(built, types, variant):

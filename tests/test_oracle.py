@@ -1,6 +1,8 @@
 """The FP64 CPU oracle against what pins it: unit constants derived by hand
 from the reference's formulas, analytic LBM solutions, conservation laws of
 the membrane models, and the committed golden vectors.  No GPU needed."""
+import itertools
+
 import numpy as np
 import pytest
 
@@ -171,3 +173,33 @@ def test_repulsion_conserves_momentum_and_pushes_from_walls(built):
     w.stage("repulsion")
     fw = w.read_repulsion()
     assert fw[:nv, 2].sum() > 0 and np.all(fw[nv:] == 0)
+
+
+def test_neighbour_lists_match_brute_force(orc):
+    """The oracle's neighbour lists against a direct union over the 27 tiles
+    around each tile (Python), periodic in x and y, walls in z."""
+    from hemocell_gb300 import cases
+    case = cases.mixed_box(wall=True)
+    o = orc.apply_case(case, threads=1)
+    o.step(2)
+    tile = (4, 4, 4)
+    b = o.bins(tile, None, case.dims)
+    nt3 = [-(-case.dims[a] // tile[a]) for a in range(3)]
+    tco, tc = b["tile_cell_offsets"], b["tile_cells"]
+    off, cells = o.neighbours(tile, None, case.dims, case.periodic)
+    expect_off, expect = [0], []
+    for t in range(nt3[0] * nt3[1] * nt3[2]):
+        c0 = (t % nt3[0], (t // nt3[0]) % nt3[1], t // (nt3[0] * nt3[1]))
+        got = set()
+        for d in itertools.product((-1, 0, 1), repeat=3):
+            c = [c0[a] + d[a] for a in range(3)]
+            if any(not case.periodic[a] and not 0 <= c[a] < nt3[a] for a in range(3)):
+                continue
+            c = [c[a] % nt3[a] for a in range(3)]
+            u = c[0] + nt3[0] * (c[1] + nt3[1] * c[2])
+            got.update(tc[tco[u]:tco[u + 1]].tolist())
+        expect += sorted(got)
+        expect_off.append(len(expect))
+    assert np.array_equal(off, expect_off)
+    assert np.array_equal(cells, expect)
+    assert len(expect) > 0
