@@ -2083,6 +2083,7 @@ long long hc_estimate_device_bytes(const hc_params* p, int nvertices, int ncells
   // lattice arrays, as hc_create allocates them
   long long b = 2 * fb + 2 * Fb + 4 * N + Fb + 4 + 4 * N + N + 3 * ts * p->nz +
                 (long long)sizeof(TypeDev) * hcd::MAX_TYPES + 4;
+  b += 4 * N;  // the fluid-node list (at most every node)
   // vertex and cell arrays at the capacity growth can reach (twice the need)
   const long long vcap = std::max<long long>(2LL * nvertices, 1024);
   const long long ccap = std::max<long long>(2LL * ncells, 64);
