@@ -588,6 +588,46 @@ def test_collide_stream_variants_same_bits(built, form, shape, var, walls):
 
 
 @pytest.mark.parametrize("form", [0, 1])
+def test_64bit_index_path_matches_tiles(built, form):
+    """A lattice with 19 N >= 2^31 (512 x 512 x 432, 113.2 M nodes) runs the
+    collide-stream's 64-bit index path (general pull, no fluid-node list),
+    every other lattice here the 32-bit one.  Built as 8 x 8 periodic copies
+    of a 64 x 64 x 432 cross-section holding a wall-bounded channel, with the
+    Kolmogorov body force varying along z, every copy must hold the bits of
+    the 32-bit run on one copy after 6 steps (density and velocity of every
+    node)."""
+    import torch
+    from hemocell_gb300 import _lib as L
+    free, _ = torch.cuda.mem_get_info()
+    if free < 80 * 2 ** 30:
+        pytest.skip("needs about 60 GB of free device memory")
+    C = _cases()
+    nx, ny, nz, k = 64, 64, 432, 8
+    small_flags = C.cylinder_flags(nx, ny, nz, 24.0)
+    big_flags = np.tile(small_flags.reshape(nz, ny, nx), (1, k, k)).reshape(-1)
+    body = (2e-6, 0.0, 0.0)
+    small = C.Case("tile", (nx, ny, nz), (1, 1, 1), flags=small_flags, body_mode=L.HC_BODY_KOLMOGOROV, body=body)
+    big = C.Case("tiled", (k * nx, k * ny, nz), (1, 1, 1), flags=big_flags, body_mode=L.HC_BODY_KOLMOGOROV,
+                 body=body)
+    assert 19 * big.N >= 2 ** 31 > 19 * small.N
+    a = small.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    a.iterate(6)
+    ra, ua = a.read_fluid()
+    a.close()
+    b = big.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    b.iterate(6)
+    rb, ub = b.read_fluid()
+    assert b.device_status() == 0
+    b.close()
+    assert np.abs(ua).max() > 0          # the force has set the fluid moving
+    ra = ra.reshape(nz, 1, ny, 1, nx)
+    assert np.array_equal(rb.reshape(nz, k, ny, k, nx), np.broadcast_to(ra, (nz, k, ny, k, nx)))
+    del rb
+    ua = ua.reshape(3, nz, 1, ny, 1, nx)
+    assert np.array_equal(ub.reshape(3, nz, k, ny, k, nx), np.broadcast_to(ua, (3, nz, k, ny, k, nx)))
+
+
+@pytest.mark.parametrize("form", [0, 1])
 def test_profile_kernels_times_the_step(built, form):
     """hc_profile_kernels runs the step hc_step runs: the state it leaves is
     the state of as many plain steps (3 queued + nsteps), and its kernel
