@@ -628,6 +628,58 @@ def test_64bit_index_path_matches_tiles(built, form):
 
 
 @pytest.mark.parametrize("form", [0, 1])
+def test_64bit_index_path_with_a_cell(built, form):
+    """The cell stages' 64-bit index paths (tagged node velocity, spread,
+    interpolation, force assembly on a lattice with 19 N >= 2^31): the tiled
+    channels of the test above, with one RBC in copy (3, 5), against the same
+    RBC in one copy (positions shifted by whole tiles, which changes their
+    rounding: within the run tolerance) and an empty copy (every other copy
+    of the big lattice, bit for bit), after 10 steps."""
+    import torch
+    from hemocell_gb300 import _lib as L
+    free, _ = torch.cuda.mem_get_info()
+    if free < 80 * 2 ** 30:
+        pytest.skip("needs about 60 GB of free device memory")
+    C = _cases()
+    nx, ny, nz, k, tx, ty = 64, 64, 432, 8, 3, 5
+    small_flags = C.cylinder_flags(nx, ny, nz, 24.0)
+    big_flags = np.tile(small_flags.reshape(nz, ny, nx), (1, k, k)).reshape(-1)
+    body = (2e-6, 0.0, 0.0)
+    t = C.rbc_type(600)
+    xyz = C.place_cells(t.mesh, np.array([[31.5, 31.5, 200.0]]), np.array([[0.3, -0.2, 0.5]]))
+    offset = np.array([tx * nx, ty * ny, 0.0])
+    kw = dict(periodic=(1, 1, 1), body_mode=L.HC_BODY_KOLMOGOROV, body=body)
+    runs = {}
+    for name, dims, flags, cells in (("cell", (nx, ny, nz), small_flags, [(0, xyz)]),
+                                     ("empty", (nx, ny, nz), small_flags, []),
+                                     ("big", (k * nx, k * ny, nz), big_flags, [(0, xyz + offset)])):
+        case = C.Case(name, dims, kw["periodic"], flags=flags, body_mode=kw["body_mode"], body=kw["body"],
+                      types=[t] if cells else [], cells=cells)
+        h = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+        h.iterate(10)
+        runs[name] = (h.read_vertices()[0] if cells else None, h.read_fluid(), h.device_status())
+        h.close()
+    tol = RUN_TOL if form == 0 else 1e-5
+    xa, (ra, ua), sa = runs["cell"]
+    _, (rc, uc), _ = runs["empty"]
+    xb, (rb, ub), sb = runs["big"]
+    assert sa == sb == 0
+    assert rel_l2(xb - offset, xa) < tol
+    assert np.abs(xa - xyz).max() > 0                 # the cell has moved
+    rb = rb.reshape(nz, k, ny, k, nx)
+    ub = ub.reshape(3, nz, k, ny, k, nx)
+    assert rel_l2(ub[:, :, ty, :, tx, :].reshape(-1), ua.reshape(-1)) < tol
+    assert rel_l2(rb[:, ty, :, tx, :].reshape(-1), ra) < tol
+    rc = rc.reshape(nz, ny, nx)
+    uc = uc.reshape(3, nz, ny, nx)
+    for j in range(k):
+        for i in range(k):
+            if (i, j) != (tx, ty):
+                assert np.array_equal(rb[:, j, :, i, :], rc)
+                assert np.array_equal(ub[:, :, j, :, i, :], uc)
+
+
+@pytest.mark.parametrize("form", [0, 1])
 def test_profile_kernels_times_the_step(built, form):
     """hc_profile_kernels runs the step hc_step runs: the state it leaves is
     the state of as many plain steps (3 queued + nsteps), and its kernel
