@@ -588,6 +588,37 @@ def test_collide_stream_variants_same_bits(built, form, shape, var, walls):
 
 
 @pytest.mark.parametrize("form", [0, 1])
+@pytest.mark.parametrize("dims,periodic,fill", [((1, 1, 1), (1, 1, 1), 0), ((2, 3, 1), (1, 1, 1), 0),
+                                               ((1, 5, 4), (1, 1, 1), 0), ((4, 3, 1), (1, 1, 0), 0),
+                                               ((5, 2, 6), (1, 0, 1), 0), ((6, 5, 4), (1, 1, 1), 1)])
+def test_degenerate_lattices_against_oracle(built, form, dims, periodic, fill):
+    """Lattices of one or two nodes along an axis, periodic (every pull wraps
+    onto the node itself or its one neighbour) and not (every link off a
+    one-node axis bounces back), from random populations under a uniform body
+    force: 20 graph-replayed steps against the oracle.  A lattice of wall
+    nodes only steps without error."""
+    from hemocell_gb300 import _lib as L
+    C = _cases()
+    n = dims[0] * dims[1] * dims[2]
+    flags = np.full(n, fill, np.uint8)
+    case = C.Case("tiny", dims, periodic, flags=flags, body_mode=L.HC_BODY_UNIFORM, body=(2e-5, -1e-5, 3e-5))
+    hc = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+    o = _orc().apply_case(case)
+    randomize(case, hc, o)
+    hc.iterate(20)
+    o.step(20)
+    assert hc.device_status() == 0
+    rg, ug = hc.read_fluid()
+    hc.close()
+    if fill:
+        return
+    ro, uo = o.read_fluid()
+    tol = RUN_TOL if form == 0 else 1e-5
+    assert rel_l2(rg, ro) < tol
+    assert rel_l2(ug, uo) < tol
+
+
+@pytest.mark.parametrize("form", [0, 1])
 def test_64bit_index_path_matches_tiles(built, form):
     """A lattice with 19 N >= 2^31 (512 x 512 x 432, 113.2 M nodes) runs the
     collide-stream's 64-bit index path (general pull, no fluid-node list),
