@@ -497,7 +497,11 @@ __global__ void __launch_bounds__(256) k_node_velocity_packed(const LbmView<T> L
 // layout: whole warps of coalesced pulls, where the tagged forms pull only
 // the stencil nodes through partly used sectors.  Interpolation reads only
 // tagged nodes, whose values are the tagged forms' bits.  Needs 19 N < 2^31.
-template <typename T, bool MW>
+// INTERIOR: interior nodes take pull_interior, as the collide-stream does
+// with tune[7] bit 12.  Without it every node takes pull_inline: a warp that
+// holds both kinds of node (every warp of a lattice with walls across its
+// rows) then issues one sequence of 19 loads instead of both.
+template <typename T, bool MW, bool INTERIOR>
 __global__ void __launch_bounds__(256) k_node_velocity_dense(const LbmView<T> L) {
   pdl_wait();
   const int X = blockIdx.x * blockDim.x + threadIdx.x;
@@ -508,7 +512,7 @@ __global__ void __launch_bounds__(256) k_node_velocity_dense(const LbmView<T> L)
   const uint32_t m = __ldg(L.nbmask + n);
   if (m & NB_SOLID) return;
   T f[19];
-  if (m & NB_INTERIOR) pull_interior(L, L.fsrc, n, f);
+  if (INTERIOR && (m & NB_INTERIOR)) pull_interior(L, L.fsrc, n, f);
   else if (pull_is_inline(L, X, Y, Z, m)) pull_inline<T, MW>(L, L.fsrc, n, X, Y, Z, m, f);
   else pull(L, L.fsrc, X, Y, Z, (long long)n, m, f);
   T rhoBar, jx, jy, jz, Fx, Fy, Fz;
@@ -523,8 +527,12 @@ __global__ void __launch_bounds__(256) k_node_velocity_dense(const LbmView<T> L)
 template <typename T>
 cudaError_t launch_node_velocity_dense(const LbmView<T>& L, cudaStream_t s) {
   const dim3 b(32, 8), g((L.nx + 31) / 32, (L.ny + 7) / 8, L.nz);
-  if (L.moving_walls) return launch_kernel(k_node_velocity_dense<T, true>, g, b, 0, s, L.pdl, L);
-  return launch_kernel(k_node_velocity_dense<T, false>, g, b, 0, s, L.pdl, L);
+  switch ((L.k1var & 1) | (L.moving_walls ? 2 : 0)) {
+    case 0: return launch_kernel(k_node_velocity_dense<T, false, false>, g, b, 0, s, L.pdl, L);
+    case 1: return launch_kernel(k_node_velocity_dense<T, false, true>, g, b, 0, s, L.pdl, L);
+    case 2: return launch_kernel(k_node_velocity_dense<T, true, false>, g, b, 0, s, L.pdl, L);
+    default: return launch_kernel(k_node_velocity_dense<T, true, true>, g, b, 0, s, L.pdl, L);
+  }
 }
 
 template <typename T>

@@ -67,8 +67,9 @@ def test_collide_stream_one_stage(built):
 def _k1_codes():
     # 1: one thread per fluid node; 0x100: node velocity per fluid node;
     # 0x200: node velocity over warp-packed tagged nodes; 0x300: node velocity
-    # at every fluid node; bulk collide-stream: stages | CTAs per SM << 4
-    return [1, 0x101, 0x200, 0x201, 0x300, 0x301, 3 | (1 << 4), 4 | (2 << 4), 2 | (3 << 4)]
+    # at every fluid node (0x1300: with the interior pull of bit 12); bulk
+    # collide-stream: stages | CTAs per SM << 4
+    return [1, 0x101, 0x200, 0x201, 0x300, 0x301, 0x1300, 3 | (1 << 4), 4 | (2 << 4), 2 | (3 << 4)]
 
 
 @pytest.mark.parametrize("form", [0, 1])
