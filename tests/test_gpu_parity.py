@@ -711,6 +711,36 @@ def test_64bit_index_path_with_a_cell(built, form):
                 assert np.array_equal(ub[:, :, j, :, i, :], uc)
 
 
+def test_autotune_restores_state_and_caches(built, tmp_path):
+    """hc_autotune leaves the state as it found it, picks a valid tuning whose
+    run matches the default tuning's (FP32 within 1e-5), and a second handle
+    of the same case reads that pick from the cache file."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=True)
+    a = case.build(form=1, launch=L.HC_LAUNCH_BATCHED)
+    b = case.build(form=1, launch=L.HC_LAUNCH_BATCHED)
+    a.iterate(5)
+    b.iterate(5)
+    x0 = b.read_vertices()[0]
+    f0 = b.read_fluid()[1]
+    cache = str(tmp_path / "tuning.txt")
+    b.autotune(cache)
+    assert np.array_equal(b.read_vertices()[0], x0)
+    assert np.array_equal(b.read_fluid()[1], f0)
+    t = b.tuning()
+    b.set_tuning(t)
+    a.iterate(20)
+    b.iterate(20)
+    assert rel_l2(b.read_vertices()[0], a.read_vertices()[0]) < 1e-5
+    assert rel_l2(b.read_fluid()[1], a.read_fluid()[1]) < 1e-5
+    assert b.device_status() == a.device_status()
+    c = case.build(form=1, launch=L.HC_LAUNCH_BATCHED)
+    c.autotune(cache)
+    assert c.tuning() == t
+    for h in (a, b, c):
+        h.close()
+
+
 @pytest.mark.parametrize("form", [0, 1])
 def test_profile_kernels_times_the_step(built, form):
     """hc_profile_kernels runs the step hc_step runs: the state it leaves is
