@@ -15,7 +15,9 @@ Arms:
                      all host cores.
 
 One JSON line on stdout.  Timing: CUDA events on the handle's stream around
-exactly K steps after W warm-up steps; the per-step working set (~190 MB in
+exactly K steps after W warm-up steps, that K-step region repeated until the
+repeats span at least half a second (the line reports the median, with the
+clock samples of the whole window); the per-step working set (~190 MB in
 FP32, ~370 MB in FP64) exceeds the 129 MB L2, so no flush is inserted.
 """
 from __future__ import annotations
@@ -42,13 +44,35 @@ sys.path.insert(0, ROOT)
 # algorithmic bytes per fluid node and per vertex of one step
 BYTES_NODE = {"f32": 2 * 19 * 4 + 2 * 3 * 4, "f64": 2 * 19 * 8 + 2 * 3 * 8}
 BYTES_VERTEX = {"f32": 2 * 3 * 8 + 2 * 2 * 3 * 4, "f64": 2 * 3 * 3 * 8}
-# DRAM bytes of one collide-stream launch on this workload, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum of the 64x64x256 pipe with 279
-# RBC): FP32 inside graph-replayed steps (one pass, caches as the previous
-# kernel left them, mean of 4 launches), FP64 from a --set full capture of the
-# tuned FP64 kernel; the summaries are in profiles/
-PIPE_WORKLOAD = "pipe_ht25 64x64x256 D3Q19, R=30 cylinder, 279 RBC (642 vertices), 25% Ht"
-K1_TRAFFIC_PER_LAUNCH = {"f32": 84.17e6 + 67.79e6, "f64": 178.035456e6 + 89.346560e6}
+# node velocity: 19 populations pulled, the force and the mask read, the
+# velocity written (float4 in FP32, three doubles in FP64)
+BYTES_NODE_VELOCITY = {"f32": 19 * 4 + 16 + 4 + 16, "f64": 19 * 8 + 24 + 4 + 24}
+PIPE_WORKLOAD = ("pipe_ht25 64x64x256 D3Q19, R=30 cylinder, 279 RBC (642 vertices, 81 um^3 each), 25% Ht "
+                 "of the lumen by mesh volume")
+# The reference's `Volume` key (90 um^3, examples/oneCellShear/RBC.xml) is read
+# by no code; its own haematocrit printouts count 77 um^3 per RBC
+# (cases/performance_testing/performance_testing.cpp:122).  The Evans-Fung
+# shape of R = 3.91 um encloses 81.76 um^3 and its 1280-face mesh 81.05 um^3,
+# which sets the pipe's 279 cells (about 250 at 90 um^3).
+RBC_VOLUME_NOTE = "RBC 81.05 um^3 (Evans-Fung mesh, R=3.91 um); 279 cells, ~250 at the unused Volume key's 90 um^3"
+PROFILE_TRAFFIC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                               "step_kernels_pipe_ht25_64x64x256.md")
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` (dram__bytes_read.sum +
+    dram__bytes_write.sum inside graph-replayed pipe steps) from the committed
+    ncu summary, whose lines "TRAFFIC <kernel> <bytes> <commit>" state the
+    source commit; None when the summary has no such line."""
+    try:
+        with open(PROFILE_TRAFFIC) as fh:
+            for line in fh:
+                parts = line.split()
+                if len(parts) >= 3 and parts[0] == "TRAFFIC" and parts[1] == kernel:
+                    return float(parts[2]), (parts[3] if len(parts) > 3 else None)
+    except OSError:
+        pass
+    return None, None
 
 
 def cpu_model() -> str:
@@ -91,6 +115,14 @@ class ClockSampler:
         self.samples = []
         self.proc = None
 
+    def wait_first(self, timeout: float = 3.0):
+        """Block until the first sample has arrived (nvidia-smi takes a moment
+        to start), so that the samples cover the timed window."""
+        t0 = time.perf_counter()
+        while self.proc and not self.samples and time.perf_counter() - t0 < timeout:
+            time.sleep(0.01)
+        return self
+
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -127,7 +159,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for s in self.samples for k in range(4) if s[4 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(self.samples), "timed_repeats": getattr(self, "repeats", None)}
 
 
 def build_case(steps: int):
@@ -137,7 +169,24 @@ def build_case(steps: int):
     return case
 
 
+MIN_SPAN_S = 0.5
+
+
+def repeat_timed(fn, min_span_s: float = MIN_SPAN_S, min_repeats: int = 3, max_repeats: int = 100000):
+    """Run fn() (which times one K-step region and returns its ms) until the
+    repeats span min_span_s of wall time; returns the list of timings."""
+    out = []
+    t0 = time.perf_counter()
+    while len(out) < max_repeats:
+        out.append(fn())
+        if len(out) >= min_repeats and time.perf_counter() - t0 >= min_span_s:
+            break
+    return out
+
+
 def time_form(case, form, launch, steps, warmup, tune_cache):
+    """Median device time (ms) of `steps` steps over repeats spanning half a
+    second, with the clock samples of that window."""
     from hemocell_gb300 import _lib as L
     hc = case.build(form=form, launch=launch)
     if tune_cache is not None:
@@ -145,7 +194,10 @@ def time_form(case, form, launch, steps, warmup, tune_cache):
     hc.iterate(warmup)
     hc.sync()
     with ClockSampler() as cs:
-        ms = hc.time_steps(steps)
+        cs.wait_first()
+        reps = repeat_timed(lambda: hc.time_steps(steps))
+    ms = statistics.median(reps)
+    cs.repeats = len(reps)
     # each kernel's device time inside the step as the graph runs it (events
     # on the handle's stream, launches queued ahead of the GPU)
     prof = hc.profile_kernels(200)
@@ -181,9 +233,13 @@ def e2e_form(case, form, launch, steps, warmup):
         hc.wait_positions((n - 1) & 1)
 
     run(warmup)
-    t0 = time.perf_counter()
-    run(steps)
-    dt = time.perf_counter() - t0
+
+    def one():
+        t0 = time.perf_counter()
+        run(steps)
+        return time.perf_counter() - t0
+
+    dt = statistics.median(repeat_timed(one))
     hc.close()
     h2d = 3 * case.dims[2] * (4 if form == L.HC_FORM_MIXED_F32 else 8)
     d2h = V * 3 * 8
@@ -344,13 +400,25 @@ def serving_leg(args):
     }
 
 
+def pipe_config(case, nvertices: int) -> dict:
+    """The `config` of both arms: the workload only (the arithmetic of each
+    arm is in its top-level `form`)."""
+    return {"workload": PIPE_WORKLOAD, "nodes": case.N, "fluid_nodes": int((case.flags_array() == 0).sum()),
+            "vertices": nvertices, "cells": len(case.cells), "rbc_volume": RBC_VOLUME_NOTE,
+            "l2": "working set per step > 129 MB L2, no flush"}
+
+
 def run_reference(args):
-    """--impl reference: the CPU restatement of the reference path, all host threads."""
+    """--impl reference: the CPU restatement of the reference path, all host
+    threads.  The workload (meshes, placement, packing) is built by the
+    oracle's own geometry, so this arm loads no part of the GPU library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    case = build_case(args.steps)
     from oracle import oracle as orc
+    from hemocell_gb300 import cases
+    case = cases.pipe_ht25(seed=1, geo=orc.geometry)
+    case.steps = args.steps
     threads = os.cpu_count() or 1
     o = orc.apply_case(case, threads=threads)
     t0 = time.perf_counter()
@@ -366,8 +434,10 @@ def run_reference(args):
         "impl": "reference", "metric": "MLUPS incl. IBM+cell forces", "value": mlups, "unit": "MLUPS",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / n * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": PIPE_WORKLOAD, "nodes": case.N,
-                   "vertices": case.nvertices, "form": "FP64 CPU restatement (oracle port)"},
+        "config": pipe_config(case, case.nvertices),
+        "form": "FP64 CPU restatement of the step (oracle port), OpenMP over all host threads",
+        "native_libraries": sorted({os.path.basename(l.split()[-1]) for l in open("/proc/self/maps")
+                                    if l.rstrip().endswith(".so") and ROOT in l}),
         "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
                          "sample": f"{n} full steps of the workload (of {args.steps} requested) after "
                                    f"{args.warmup} warm-up"},
@@ -426,26 +496,48 @@ def main():
     ms_max = max_over_ranks(ms)
     value = replicas_mlups(world, case.N, args.steps, ms_max)
     peak, peak_kind = measured_peaks()
-    k1_ms = prof["collide_stream"]
-    k1_bytes = fluid * BYTES_NODE["f32"]
-    achieved = k1_bytes / (k1_ms * 1e-3) / 1e9
-    traffic = K1_TRAFFIC_PER_LAUNCH["f32"]
     step_bytes = fluid * BYTES_NODE["f32"] + st.vertices * BYTES_VERTEX["f32"]
     step_gbs = step_bytes / (ms / args.steps * 1e-3) / 1e9
+    # each kernel of the step against HBM: algorithmic bytes of one launch over
+    # its live time inside the step
+    kernel_bytes = {"collide_stream": fluid * BYTES_NODE["f32"],
+                    "node_velocity": fluid * BYTES_NODE_VELOCITY["f32"],
+                    "mechanics": st.vertices * BYTES_VERTEX["f32"]}
+    kernel_names = {"collide_stream": "k_collide_stream<float>", "node_velocity": "k_node_velocity_dense<float>",
+                    "mechanics": "k_mechanics<float>"}
+    kernels = {}
+    for k, b in kernel_bytes.items():
+        gbs = b / (prof[k] * 1e-3) / 1e9
+        tr, tr_commit = profiled_traffic(kernel_names[k])
+        kernels[k] = {"kernel": kernel_names[k], "launch_ms": prof[k], "share": prof[k] / prof["step"],
+                      "algorithmic_bytes_per_launch": b, "achieved_gbs": gbs, "frac": gbs / peak,
+                      "traffic": tr, "traffic_commit": tr_commit}
+    dominant = max(kernel_bytes, key=lambda k: prof[k])
+    dom = kernels[dominant]
 
     extra = {}
     if not args.no_plain:
-        ms64, prof64, _, _, status64, tuning64 = time_form(case, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_PER_STAGE,
-                                                          args.steps, args.warmup, tune_cache)
+        ms64, prof64, clocks64, _, status64, tuning64 = time_form(case, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_PER_STAGE,
+                                                                  args.steps, args.warmup, tune_cache)
         mlups64 = case.N * args.steps / (ms64 * 1e3)
         extra["fp64_plain"] = {"value": mlups64, "unit": "MLUPS", "ms_per_step": ms64 / args.steps,
-                               "kernels_ms": prof64, "tuning": tuning64, "status": status64}
+                               "launch": "per stage", "kernels_ms": prof64, "tuning": tuning64,
+                               "status": status64, "clocks": clocks64}
         extra["fp32_batched_over_fp64_plain"] = value / world / mlups64
+        # the precision-matched form: FP64 batched (graph), on the device and
+        # through the public API with host copies
+        msb, profb, clocksb, _, statusb, tuningb = time_form(case, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_BATCHED,
+                                                             args.steps, args.warmup, tune_cache)
+        e64_dt, e64_h2d, e64_d2h = e2e_form(case, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_BATCHED, args.steps,
+                                            args.warmup)
+        extra["fp64_batched"] = {
+            "value": case.N * args.steps / (msb * 1e3), "unit": "MLUPS", "ms_per_step": msb / args.steps,
+            "kernels_ms": profb, "tuning": tuningb, "status": statusb, "clocks": clocksb,
+            "e2e": {"value": case.N * args.steps / e64_dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": e64_h2d,
+                    "d2h_bytes_per_step": e64_d2h}}
 
-    e2e_dt, h2d, d2h = e2e_form(case, L.HC_FORM_MIXED_F32, L.HC_LAUNCH_BATCHED, max(20, args.steps // 4),
-                                args.warmup)
-    e2e_steps = max(20, args.steps // 4)
-    e2e_val = world * case.N * e2e_steps / e2e_dt / 1e6
+    e2e_dt, h2d, d2h = e2e_form(case, L.HC_FORM_MIXED_F32, L.HC_LAUNCH_BATCHED, args.steps, args.warmup)
+    e2e_val = world * case.N * args.steps / e2e_dt / 1e6
 
     if not args.no_mixed_error:
         extra["mixed_vs_fp64"] = mixed_error_leg(case)
@@ -471,6 +563,11 @@ def main():
             cpu["kolmogorov_128"] = {"value": v3, "unit": "MLUPS", "sample": f"{n3} steps of the 128^3 suspension"}
     if "kolmogorov" in extra:
         extra["kolmogorov"].pop("_case", None)
+    if cpu is not None and "fp64_batched" in extra:
+        # like for like: the same FP64 arithmetic on the GPU and on the host cores
+        fb = extra["fp64_batched"]
+        fb["over_cpu"] = fb["value"] / cpu["value"]
+        fb["e2e_over_cpu"] = fb["e2e"]["value"] / cpu["value"]
 
     if rank == 0:
         line = {
@@ -478,19 +575,16 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": PIPE_WORKLOAD,
-                       "form": "mixed FP32 populations f_i-w_i / FP64 positions+volume, batched + CUDA graph",
-                       "nodes": case.N, "fluid_nodes": fluid, "vertices": st.vertices, "cells": st.cells,
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "working set per step > 129 MB L2, no flush"},
+            "config": pipe_config(case, st.vertices),
+            "form": "mixed FP32 populations f_i-w_i / FP64 positions+volume, batched + CUDA graph",
+            "parallelism": "replicas" if world > 1 else "single",
             "fluid_mlups": world * fluid * args.steps / (ms_max * 1e3),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_collide_stream<float>",
-                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": k1_bytes,
-                         "launch_ms": k1_ms,
-                         # the same with every lattice node counted (the wall nodes' populations
-                         # are neither read nor written here, so this credits bytes not moved)
-                         "frac_all_nodes": case.N * BYTES_NODE["f32"] / (k1_ms * 1e-3) / 1e9 / peak},
+            # the dominant kernel of the step (the largest live time)
+            "roofline": {"bound": "hbm", "achieved": dom["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": dom["frac"], "traffic": dom["traffic"], "kernel": dom["kernel"],
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": dom["algorithmic_bytes_per_launch"],
+                         "launch_ms": dom["launch_ms"], "share_of_step": dom["share"]},
+            "kernels_roofline": kernels,
             "step_roofline": {"bytes_per_step": step_bytes, "achieved_gbs": step_gbs, "frac": step_gbs / peak,
                               # N (all nodes) x 176 B + V x 72 B per step
                               "frac_all_nodes": (case.N * BYTES_NODE["f32"] + st.vertices * 72) /

@@ -81,6 +81,7 @@ SIGNATURES = {
                                    C.c_int]),
     "hc_add_cells": (C.c_int, [P, C.c_int, C.c_int, D, D]),
     "hc_add_cells_xyz": (C.c_int, [P, C.c_int, C.c_int, D]),
+    "hc_load_cells": (C.c_int, [P, C.c_int, C.c_int, D, D, I]),
     "hc_set_timescales": (C.c_int, [P, I, C.c_int, C.c_int]),
     "hc_set_vertex_forces": (C.c_int, [P, C.c_int, I, D]),
     "hc_set_repulsion": (C.c_int, [P, C.c_double, C.c_double, C.c_int]),

@@ -41,7 +41,9 @@ def _compile(unit: str, hdr_mtime: float, verbose: bool) -> str:
     cmd = [_nvcc(), GENCODE, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
            "-I", CSRC, "-c", src, "-o", obj]
     if unit.endswith(".cpp"):
-        cmd[1:1] = ["-x", "c++"]
+        # host geometry without fused multiply-adds: the same doubles on x86-64
+        # and aarch64, and the same as the FP64 CPU restatement's
+        cmd[1:1] = ["-x", "c++", "-Xcompiler", "-ffp-contract=off"]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -15,13 +15,22 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
+from types import SimpleNamespace
 from typing import List, Optional, Tuple
 
 import numpy as np
 
 from . import _lib as L
 from .hemocell import HemoCell, Material, Mesh, antipodal_pairs, ellipsoid_mesh, icosphere, pack_cells, \
-    place_cells, rbc_mesh
+    place_cells, pos_to_lattice, rbc_mesh
+
+# The geometry functions a workload is built with.  PRODUCT is this library's
+# (host code of libhcgpu.so); a checker may pass any object with the same
+# functions, e.g. an independent restatement, to build the same workload
+# without this library.
+PRODUCT = SimpleNamespace(icosphere=icosphere, rbc_mesh=rbc_mesh, ellipsoid_mesh=ellipsoid_mesh,
+                          antipodal_pairs=antipodal_pairs, place_cells=place_cells, pack_cells=pack_cells,
+                          pos_to_lattice=pos_to_lattice)
 
 DX = 0.5e-6
 DT = 1e-7
@@ -107,21 +116,21 @@ def seeded_angles(seed: int, n: int) -> np.ndarray:
     return np.array([[(next(g) / 2 ** 53) * 2 * math.pi - math.pi for _ in range(3)] for _ in range(n)])
 
 
-def rbc_type(min_triangles: int = 600) -> CellTypeSpec:
-    mesh = rbc_mesh(min_triangles, RBC_MATERIAL.radius / DX)
+def rbc_type(min_triangles: int = 600, geo=PRODUCT) -> CellTypeSpec:
+    mesh = geo.rbc_mesh(min_triangles, RBC_MATERIAL.radius / DX)
     return CellTypeSpec("RBC", L.HC_MODEL_RBC_HIGH_ORDER, RBC_MATERIAL, mesh)
 
 
-def plt_type(min_triangles: int = 320, radius_m: float = 1.0e-6, aspect: float = 0.25) -> CellTypeSpec:
-    mesh = ellipsoid_mesh(min_triangles, radius_m / DX, aspect)
-    mesh.inner = antipodal_pairs(mesh.xyz)
+def plt_type(min_triangles: int = 320, radius_m: float = 1.0e-6, aspect: float = 0.25, geo=PRODUCT) -> CellTypeSpec:
+    mesh = geo.ellipsoid_mesh(min_triangles, radius_m / DX, aspect)
+    mesh.inner = geo.antipodal_pairs(mesh.xyz)
     mat = Material(**{**PLT_MATERIAL.__dict__, "radius": radius_m})
     return CellTypeSpec("PLT", L.HC_MODEL_PLT_SIMPLE, mat, mesh)
 
 
-def wbc_type(min_triangles: int = 5120) -> CellTypeSpec:
-    mesh = icosphere(min_triangles, WBC_MATERIAL.radius / DX)
-    mesh.inner = antipodal_pairs(mesh.xyz)
+def wbc_type(min_triangles: int = 5120, geo=PRODUCT) -> CellTypeSpec:
+    mesh = geo.icosphere(min_triangles, WBC_MATERIAL.radius / DX)
+    mesh.inner = geo.antipodal_pairs(mesh.xyz)
     return CellTypeSpec("WBC", L.HC_MODEL_WBC_HIGH_ORDER, WBC_MATERIAL, mesh)
 
 
@@ -137,13 +146,13 @@ def shear_walls(n: Tuple[int, int, int], shear_rate: float) -> Tuple[np.ndarray,
 
 
 def shear_single_rbc(n: int = 50, shear_rate: float = 100.0, seed: int = 1, min_triangles: int = 600,
-                     steps: int = 1000) -> Case:
+                     steps: int = 1000, geo=PRODUCT) -> Case:
     """Single RBC in Couette shear (examples/oneCellShear analogue)."""
     dims = (n, n, n)
     flags, walls = shear_walls(dims, shear_rate)
-    t = rbc_type(min_triangles)
+    t = rbc_type(min_triangles, geo)
     centre = np.array([[(n - 1) / 2.0] * 3])
-    xyz = place_cells(t.mesh, centre, seeded_angles(seed, 1))
+    xyz = geo.place_cells(t.mesh, centre, seeded_angles(seed, 1))
     return Case(f"shear_rbc_{n}", dims, (1, 1, 0), flags=flags, walls=walls, types=[t], cells=[(0, xyz)],
                 steps=steps)
 
@@ -158,17 +167,18 @@ def cylinder_flags(nx: int, ny: int, nz: int, radius: float) -> np.ndarray:
 
 def pipe_ht25(nx: int = 64, ny: int = 64, nz: int = 256, radius: float = 30.0, ht: float = 0.25,
               u_max_phys: float = 1e-3, seed: int = 1, min_triangles: int = 600, steps: int = 2000,
-              n_cells: Optional[int] = None) -> Case:
+              n_cells: Optional[int] = None, geo=PRODUCT) -> Case:
     """Pipe flow at a given hematocrit (examples/pipeflow analogue): body force
     F_z = 4 nu u_max / R^2 (Poiseuille), RBCs packed >= 1 lu from the wall."""
     flags = cylinder_flags(nx, ny, nz, radius)
-    t = rbc_type(min_triangles)
+    t = rbc_type(min_triangles, geo)
     vol = _mesh_volume(t.mesh)
     lumen = float((flags == 0).sum())
     if n_cells is None:
         n_cells = int(round(ht * lumen / vol))
-    centres, angles, types = pack_cells((nx, ny, nz), (1, 1, 1), flags, [t.mesh], [n_cells], margin=1.0, seed=seed)
-    xyz = place_cells(t.mesh, centres, angles)
+    centres, angles, types = geo.pack_cells((nx, ny, nz), (1, 1, 1), flags, [t.mesh], [n_cells], margin=1.0,
+                                            seed=seed)
+    xyz = geo.place_cells(t.mesh, centres, angles)
     nv = t.mesh.nv
     cells = [(0, xyz[k * nv:(k + 1) * nv]) for k in range(centres.shape[0])]
     nu = (1.0 - 0.5) / 3.0
@@ -180,21 +190,22 @@ def pipe_ht25(nx: int = 64, ny: int = 64, nz: int = 256, radius: float = 30.0, h
 
 def kolmogorov_mix(n: int = 128, rbc_fraction: float = 0.30, n_wbc: int = 2, plt_per_rbc: float = 0.1,
                    u_peak: float = 5e-3, seed: int = 1, steps: int = 1000, rbc_triangles: int = 600,
-                   plt_triangles: int = 320, wbc_triangles: int = 5120) -> Case:
+                   plt_triangles: int = 320, wbc_triangles: int = 5120, geo=PRODUCT) -> Case:
     """Heterogeneous suspension in a periodic cube with Kolmogorov forcing
     F_x = A sin(2 pi z / n), A = u_peak nu k^2 (cases/kolmogorovFlow analogue)."""
     dims = (n, n, n)
-    types = [rbc_type(rbc_triangles), plt_type(plt_triangles), wbc_type(wbc_triangles)]
+    types = [rbc_type(rbc_triangles, geo), plt_type(plt_triangles, geo=geo), wbc_type(wbc_triangles, geo)]
     n_rbc = int(round(rbc_fraction * n ** 3 / _mesh_volume(types[0].mesh)))
     n_plt = int(round(plt_per_rbc * n_rbc))
     counts = [n_rbc, n_plt, n_wbc]
-    centres, angles, tids = pack_cells(dims, (1, 1, 1), None, [t.mesh for t in types], counts, margin=0.0, seed=seed)
+    centres, angles, tids = geo.pack_cells(dims, (1, 1, 1), None, [t.mesh for t in types], counts, margin=0.0,
+                                           seed=seed)
     cells = []
     for t in range(3):
         sel = np.where(tids == t)[0]
         if len(sel) == 0:
             continue
-        xyz = place_cells(types[t].mesh, centres[sel], angles[sel])
+        xyz = geo.place_cells(types[t].mesh, centres[sel], angles[sel])
         nv = types[t].mesh.nv
         cells += [(t, xyz[k * nv:(k + 1) * nv]) for k in range(len(sel))]
     nu = (1.0 - 0.5) / 3.0
@@ -203,7 +214,7 @@ def kolmogorov_mix(n: int = 128, rbc_fraction: float = 0.30, n_wbc: int = 2, plt
                 types=types, cells=cells, steps=steps)
 
 
-def mixed_box(seed: int = 5, n: Tuple[int, int, int] = (20, 18, 16), wall: bool = True) -> Case:
+def mixed_box(seed: int = 5, n: Tuple[int, int, int] = (20, 18, 16), wall: bool = True, geo=PRODUCT) -> Case:
     """Small box with one cell of each type (RBC 162, PLT 42, WBC 162 vertices)
     and, optionally, moving walls: the stage-by-stage parity case."""
     nx, ny, nz = n
@@ -212,44 +223,49 @@ def mixed_box(seed: int = 5, n: Tuple[int, int, int] = (20, 18, 16), wall: bool 
         periodic = (1, 1, 0)
     else:
         flags, walls, periodic = None, {}, (1, 1, 1)
-    types = [rbc_type(320), plt_type(80, radius_m=1.0e-6, aspect=0.4), wbc_type(320)]
+    types = [rbc_type(320, geo), plt_type(80, radius_m=1.0e-6, aspect=0.4, geo=geo), wbc_type(320, geo)]
     rng = np.random.default_rng(seed)
     cells = []
     centres = [((nx - 1) / 2, (ny - 1) / 2 - 3.5, (nz - 1) / 2), ((nx - 1) / 2 + 4, (ny - 1) / 2 + 5, (nz - 1) / 2),
                ((nx - 1) / 2 - 4.5, (ny - 1) / 2 + 4.0, (nz - 1) / 2 + 1)]
     for t, c in enumerate(centres):
         ang = rng.uniform(-np.pi, np.pi, size=(1, 3))
-        xyz = place_cells(types[t].mesh, np.array([c]), ang)
+        xyz = geo.place_cells(types[t].mesh, np.array([c]), ang)
         cells.append((t, xyz))
     return Case("mixed_box", n, periodic, flags=flags, walls=walls, types=types, cells=cells,
                 body_mode=1, body=(2e-6, -1e-6, 5e-7))
 
 
-def repulsion_box() -> Case:
+def repulsion_box(geo=PRODUCT) -> Case:
     """Two RBCs (162 vertices) stacked close together in a 24x24x16 Couette box,
     the lower one about a lattice unit from the bottom wall: the repulsion
     parity case (inter-cell pairs and wall pushes both occur)."""
     n = (24, 24, 16)
     flags, walls = shear_walls(n, 2000.0)
-    t = rbc_type(320)
-    cells = [(0, place_cells(t.mesh, np.array([[11.5, 11.5, 3.6]]), np.zeros((1, 3)))),
-             (0, place_cells(t.mesh, np.array([[12.0, 11.0, 8.2]]), np.array([[0.1, -0.05, 0.2]])))]
+    t = rbc_type(320, geo)
+    # -pi/2 about x turns the template's disc axis (y) onto z: the discs stack
+    q = -math.pi / 2
+    cells = [(0, geo.place_cells(t.mesh, np.array([[11.5, 11.5, 3.6]]), np.array([[q, 0.0, 0.0]]))),
+             (0, geo.place_cells(t.mesh, np.array([[12.0, 11.0, 8.2]]), np.array([[q + 0.1, -0.05, 0.2]])))]
     return Case("repulsion_box", n, (1, 1, 0), flags=flags, walls=walls, types=[t], cells=cells)
 
 
-def stretch_cell(min_triangles: int = 600) -> Case:
+def stretch_cell(min_triangles: int = 600, geo=PRODUCT) -> Case:
     """Single RBC in a closed 52x26x26 box (tests/validation/stretch_cell):
     nuP 1.1e-6, dt 1e-7 -> tau 1.82; box faces are static walls; the cell is
-    centred at (12, 6, 6) um with its disc in the x-y plane (axial = x,
-    transverse = y as the test measures them)."""
+    placed by the test's stretch_RBC.pos line "12.0 6 6 90 0 0" (centre in
+    micrometres, angles in degrees), which turns the template's disc axis (y)
+    onto z: the disc lies in the x-y plane (axial = x, transverse = y as the
+    test measures them)."""
     nz = 26
     dims = (2 * nz, nz, nz)
     flags = np.zeros((dims[2], dims[1], dims[0]), np.uint8)
     flags[0, :, :] = flags[-1, :, :] = 1
     flags[:, 0, :] = flags[:, -1, :] = 1
     flags[:, :, 0] = flags[:, :, -1] = 1
-    t = rbc_type(min_triangles)
-    xyz = place_cells(t.mesh, np.array([[24.0, 12.0, 12.0]]), np.zeros((1, 3)))
+    t = rbc_type(min_triangles, geo)
+    centre, angles = geo.pos_to_lattice([[12.0, 6.0, 6.0]], [[90.0, 0.0, 0.0]], DX)
+    xyz = geo.place_cells(t.mesh, centre, angles)
     tau = 3.0 * 1.1e-6 * DT / DX ** 2 + 0.5
     return Case("stretch_cell", dims, (0, 0, 0), tau=tau, flags=flags.reshape(-1), walls={1: (0.0, 0.0, 0.0)},
                 types=[t], cells=[(0, xyz)], steps=10000)

@@ -292,12 +292,19 @@ class HemoCell {
       for (long i = 0; i < n; ++i) {
         in >> c[3 * i] >> c[3 * i + 1] >> c[3 * i + 2] >> a[3 * i] >> a[3 * i + 1] >> a[3 * i + 2];
         for (int k = 0; k < 3; ++k) {
-          c[3 * i + k] *= 1e-6 / Parameters::dx;
-          a[3 * i + k] *= -M_PI / 180.0;
+          c[3 * i + k] = c[3 * i + k] * (1e-6 / Parameters::dx) + 0.0;
+          a[3 * i + k] = (a[3 * i + k] * (M_PI / 180.0)) * -1.0;
         }
       }
       if (!in) die("(readPositionsBloodCells) malformed " + f->name + ".pos");
-      if (n > 0) check(hc_add_cells(h_, f->ctype, (int)n, c.data(), a.data()));
+      if (n > 0) {
+        // cells with a vertex on a wall node or off a closed axis are left
+        // out, as positionCellInParticleField + deleteIncompleteCells do
+        const int added = hc_load_cells(h_, f->ctype, (int)n, c.data(), a.data(), nullptr);
+        check(added);
+        std::cout << "(readPositionsBloodCells) " << f->name << ": " << added << " of " << n
+                  << " cells inside the fluid" << std::endl;
+      }
     }
     pushTimescales();
   }

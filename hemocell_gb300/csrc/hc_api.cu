@@ -174,6 +174,28 @@ namespace {
     }                                                                                          \
   } while (0)
 
+// CUDA events owned by one call: destroyed on every return path, including
+// the early returns of HC_CUDA.
+template <int K>
+struct ScopedEvents {
+  cudaEvent_t e[K] = {};
+  ScopedEvents() = default;
+  ScopedEvents(const ScopedEvents&) = delete;
+  ScopedEvents& operator=(const ScopedEvents&) = delete;
+  ~ScopedEvents() {
+    for (auto& x : e)
+      if (x) cudaEventDestroy(x);
+  }
+  cudaError_t create() {
+    for (auto& x : e) {
+      cudaError_t r = cudaEventCreate(&x);
+      if (r != cudaSuccess) return r;
+    }
+    return cudaSuccess;
+  }
+  cudaEvent_t& operator[](int k) { return e[k]; }
+};
+
 int fail(hc_handle* h, int code, const std::string& msg) {
   h->err = msg;
   return code;
@@ -1066,6 +1088,14 @@ int autotune(hc_handle* h, const char* cache) {
   for (auto& pr : parts) total += (pr.second + 255) / 256 * 256;
   char* snap = nullptr;
   HC_CUDA(h, cudaMallocFromPoolAsync((void**)&snap, total, h->pool, h->stream));
+  // the snapshot goes back to the pool on every return path
+  struct SnapGuard {
+    char*& p;
+    cudaStream_t s;
+    ~SnapGuard() {
+      if (p) cudaFreeAsync(p, s);
+    }
+  } snap_guard{snap, h->stream};
   {
     size_t off = 0;
     for (auto& pr : parts) {
@@ -1087,9 +1117,9 @@ int autotune(hc_handle* h, const char* cache) {
     h->stamp_ahead = sa0;
     return HC_OK;
   };
-  cudaEvent_t ea, eb;
-  HC_CUDA(h, cudaEventCreate(&ea));
-  HC_CUDA(h, cudaEventCreate(&eb));
+  ScopedEvents<2> tev;
+  HC_CUDA(h, tev.create());
+  cudaEvent_t ea = tev[0], eb = tev[1];
   // the fastest of three timings of the same steps from the same state:
   // candidates often differ by a few percent, about the spread of one timing
   auto trial = [&]() -> float {
@@ -1234,10 +1264,9 @@ int autotune(hc_handle* h, const char* cache) {
     h->tune[6] = mv;
   }
   int rc = restore();
-  cudaEventDestroy(ea);
-  cudaEventDestroy(eb);
   HC_CUDA(h, cudaStreamSynchronize(h->stream));
   HC_CUDA(h, cudaFreeAsync(snap, h->stream));
+  snap = nullptr;
   if (rc != HC_OK) return rc;
   invalidate_graph(h);
   if (cache && *cache) {
@@ -1253,8 +1282,8 @@ template <typename T>
 int profile_stages(hc_handle* h, int nsteps, double* out) {
   int rc0 = undo_fused_spread(h);  // every profiled step spreads on its own
   if (rc0 != HC_OK) return rc0;
-  cudaEvent_t ev[5];
-  for (auto& e : ev) HC_CUDA(h, cudaEventCreate(&e));
+  ScopedEvents<5> ev;
+  HC_CUDA(h, ev.create());
   double acc[5] = {0, 0, 0, 0, 0};
   for (int k = 0; k < nsteps; ++k) {
     int rc;
@@ -1277,7 +1306,6 @@ int profile_stages(hc_handle* h, int nsteps, double* out) {
     HC_CUDA(h, cudaEventElapsedTime(&t, ev[0], ev[4]));
     acc[4] += t;
   }
-  for (auto& e : ev) cudaEventDestroy(e);
   for (int s = 0; s < 5; ++s) out[s] = nsteps > 0 ? acc[s] / nsteps : 0.0;
   return HC_OK;
 }
@@ -1688,6 +1716,50 @@ int hc_add_cells(hc_handle* h, int type, int n, const double* centres, const dou
   return rc == HC_OK ? first : rc;
 }
 
+// loadParticles' admission of one placed cell (io/readPositionsBloodCells.cpp:120-170
+// and the deleteIncompleteCells that follows it, :354): a vertex is added only
+// when it lies in the lattice's box (-0.5, n - 0.5] on every axis
+// (isContainedABS on the particle field's box; periodic axes are not
+// wrapped at loading) and its node int(x + 0.5) is not a boundary node; a
+// cell missing any vertex is deleted.  The deny layer of
+// setInitialMinimumDistanceFromSolid is an unsigned number of micrometres in
+// the reference (core/hemoCellField.h:64), so the 0.5 um its cases pass
+// truncates to 0 and only the vertex's own node is checked.
+bool cell_admitted(const hc_handle* h, const double* xyz, int nv) {
+  const int dims[3] = {h->nx, h->ny, h->nz};
+  for (int i = 0; i < nv; ++i) {
+    long long q[3];
+    for (int a = 0; a < 3; ++a) {
+      const double x = xyz[3 * i + a];
+      if (!(x > -0.5 && x <= dims[a] - 0.5)) return false;
+      q[a] = (long long)(x + 0.5);
+      if (q[a] >= dims[a]) return false;
+    }
+    if (h->hflag[(size_t)q[0] + (size_t)dims[0] * ((size_t)q[1] + (size_t)dims[1] * (size_t)q[2])]) return false;
+  }
+  return true;
+}
+
+int hc_load_cells(hc_handle* h, int type, int n, const double* centres, const double* angles, int* loaded) {
+  if (!h || n < 0 || (n > 0 && (!centres || !angles))) return HC_ERR_INVALID;
+  if (type < 0 || type >= (int)h->types.size()) return fail(h, HC_ERR_INVALID, "unknown cell type");
+  const int nv = h->types[type].tc.nv;
+  std::vector<double> keep, one;
+  int kept = 0;
+  for (int c = 0; c < n; ++c) {
+    one.clear();
+    hcg::place_cell(h->types[type].tc.rest, centres + 3 * c, angles + 3 * c, one);
+    const bool ok = cell_admitted(h, one.data(), nv);
+    if (loaded) loaded[c] = ok ? 1 : 0;
+    if (!ok) continue;
+    keep.insert(keep.end(), one.begin(), one.end());
+    ++kept;
+  }
+  if (kept == 0) return 0;
+  int rc = add_cells_positions(h, type, kept, keep);
+  return rc == HC_OK ? kept : rc;
+}
+
 int hc_add_cells_xyz(hc_handle* h, int type, int n, const double* xyz) {
   if (!h || n < 0 || (n > 0 && !xyz)) return HC_ERR_INVALID;
   if (type < 0 || type >= (int)h->types.size()) return fail(h, HC_ERR_INVALID, "unknown cell type");
@@ -1829,17 +1901,14 @@ int hc_sync(hc_handle* h) {
 
 int hc_time_steps(hc_handle* h, int nsteps, double* ms) {
   if (!h || !ms || nsteps < 0) return HC_ERR_INVALID;
-  cudaEvent_t a, b;
-  HC_CUDA(h, cudaEventCreate(&a));
-  HC_CUDA(h, cudaEventCreate(&b));
-  HC_CUDA(h, cudaEventRecord(a, h->stream));
+  ScopedEvents<2> ev;
+  HC_CUDA(h, ev.create());
+  HC_CUDA(h, cudaEventRecord(ev[0], h->stream));
   int rc = h->f64 ? run_steps<double>(h, nsteps) : run_steps<float>(h, nsteps);
-  HC_CUDA(h, cudaEventRecord(b, h->stream));
-  HC_CUDA(h, cudaEventSynchronize(b));
+  HC_CUDA(h, cudaEventRecord(ev[1], h->stream));
+  HC_CUDA(h, cudaEventSynchronize(ev[1]));
   float t = 0;
-  HC_CUDA(h, cudaEventElapsedTime(&t, a, b));
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
+  HC_CUDA(h, cudaEventElapsedTime(&t, ev[0], ev[1]));
   *ms = t;
   return rc;
 }

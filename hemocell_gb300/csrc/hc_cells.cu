@@ -1528,7 +1528,8 @@ __global__ void k_bin_fill(const int* vtile, int nvert, const int* offsets, int*
   tile_vertices[pos] = i;
 }
 
-// One CTA per tile: rank sort of the segment (keys are unique vertex ids),
+// One CTA per tile: rank sort of the segment in shared memory (keys are
+// unique vertex ids; a segment beyond 2048 takes a sorting network in place),
 // then the number of distinct cells in the sorted segment.
 __global__ void k_bin_sort(const int* offsets, int* tile_vertices, const int* vcell, int* tile_cell_counts) {
   __shared__ int buf[2048];
@@ -1570,21 +1571,40 @@ __global__ void k_bin_sort(const int* offsets, int* tile_vertices, const int* vc
     __syncthreads();
     if (threadIdx.x == 0) tile_cell_counts[t] = ncell;
   } else {
-    // large segment: serial insertion sort by one thread (rare)
-    if (threadIdx.x == 0) {
-      for (int k = b + 1; k < e; ++k) {
-        const int key = tile_vertices[k];
-        int j = k - 1;
-        while (j >= b && tile_vertices[j] > key) {
-          tile_vertices[j + 1] = tile_vertices[j];
-          --j;
+    // A segment beyond the shared buffer is sorted in place in global memory
+    // by the whole CTA: Batcher's bitonic network in its all-ascending form
+    // (each merge starts by comparing element i with its mirror in the block
+    // of size k, then halves the stride), over the length padded to a power
+    // of two with +infinity.  A pair whose upper element lies in the padding
+    // already holds the smaller key below, so it is skipped, and no index
+    // past the segment is touched.  O(len log^2 len) / blockDim.x steps.
+    int* seg = tile_vertices + b;
+    int p2 = 1;
+    while (p2 < len) p2 <<= 1;
+    for (int k = 2; k <= p2; k <<= 1) {
+      for (int j = k >> 1; j >= 1; j >>= 1) {
+        // the first pass of a merge pairs i with its mirror in the k-block,
+        // the later ones with i + j
+        for (int q = threadIdx.x; q < p2 / 2; q += blockDim.x) {
+          const int i = (q / j) * 2 * j + (q % j);       // lower element of pair q
+          const int u = (j == k >> 1) ? (i | (k - 1)) - (i & (k - 1)) : i + j;
+          if (u < len) {
+            const int a = seg[i], c = seg[u];
+            if (a > c) {
+              seg[i] = c;
+              seg[u] = a;
+            }
+          }
         }
-        tile_vertices[j + 1] = key;
+        __syncthreads();
       }
-      int c = 0;
-      for (int k = b; k < e; ++k) c += (k == b || vcell[tile_vertices[k]] != vcell[tile_vertices[k - 1]]) ? 1 : 0;
-      tile_cell_counts[t] = c;
     }
+    int local = 0;
+    for (int k = threadIdx.x; k < len; k += blockDim.x)
+      local += (k == 0 || vcell[seg[k]] != vcell[seg[k - 1]]) ? 1 : 0;
+    atomicAdd(&ncell, local);
+    __syncthreads();
+    if (threadIdx.x == 0) tile_cell_counts[t] = ncell;
   }
 }
 

@@ -135,30 +135,72 @@ Mesh icosphere(int min_triangles, double radius) {
   return m;
 }
 
-// RBC_FROM_SPHERE: spherePointToRBCPoint with R=1 followed by scale(radius)
-// (helper/meshGeneratingFunctions.hh:153-168, :213-241).  The reference's
-// fixed Palabos Euler rotation before and after the map is not applied.
+// The shape constructors' fixed rotation TriangleSet::rotate(pi/2 + a0,
+// pi/2 + a1, a2) with a0 = a1 = a2 = 0 (HemoCellField passes zero Euler
+// angles, core/hemoCellField.cpp:59-66; helper/meshGeneratingFunctions.hh:223-238).
+// The Euler angles are read in the "x-convention" (rotation by phi about z,
+// theta about the new x, psi about the new z) and applied to point
+// coordinates as p' = A p with Goldstein's matrix A = B(psi) C(theta) D(phi).
+// With (pi/2, pi/2, 0) it takes (x, y, z) to (y, z, x) up to cos(pi/2)
+// rounding: the biconcave disc's axis ends on y, which the reference's
+// stretch validation relies on (its cell is placed with angles (90, 0, 0)
+// and measured across x and y, tests/validation/stretch_cell).
+struct Euler {
+  double a[3][3];
+  Euler(double phi, double theta, double psi) {
+    const double cf = std::cos(phi), sf = std::sin(phi), ct = std::cos(theta), st = std::sin(theta);
+    const double cp = std::cos(psi), sp = std::sin(psi);
+    a[0][0] = cp * cf - ct * sf * sp;
+    a[0][1] = cp * sf + ct * cf * sp;
+    a[0][2] = sp * st;
+    a[1][0] = -sp * cf - ct * sf * cp;
+    a[1][1] = -sp * sf + ct * cf * cp;
+    a[1][2] = cp * st;
+    a[2][0] = st * sf;
+    a[2][1] = -st * cf;
+    a[2][2] = ct;
+  }
+  Vec3 operator()(Vec3 p) const {
+    return {a[0][0] * p.x + a[0][1] * p.y + a[0][2] * p.z, a[1][0] * p.x + a[1][1] * p.y + a[1][2] * p.z,
+            a[2][0] * p.x + a[2][1] * p.y + a[2][2] * p.z};
+  }
+};
+const Euler& shape_rotation() {
+  static const Euler R(M_PI / 2.0, M_PI / 2.0, 0.0);
+  return R;
+}
+
+// RBC_FROM_SPHERE (helper/meshGeneratingFunctions.hh:153-168, :213-241): the
+// unit icosphere rotated, spherePointToRBCPoint with R = 1, scale(radius),
+// the same rotation again.  Palabos's inflate() of the finished mesh
+// (helper/meshGeneratingFunctions.h:89-93) is not in the reference tree and
+// is not applied.
 Mesh rbc_from_sphere(int min_triangles, double radius) {
   Mesh m = merge_soup(icosphere_soup(min_triangles));
+  const Euler& R = shape_rotation();
   const double C0 = 0.054322, C2 = 1.001279, C4 = -0.561381;
   for (Vec3& p : m.v) {
+    p = R(p);
     double r2 = p.x * p.x + p.y * p.y;
     const int s = sgn(p.z);
     if (1 - r2 < 0) r2 = 1;
     Vec3 q = {p.x, p.y, s * std::sqrt(1 - r2) * (C0 + C2 * r2 + C4 * r2 * r2)};
-    p = mul(q, radius);
+    p = R(mul(q, radius));
   }
   return m;
 }
 
-// ELLIPSOID_FROM_SPHERE (helper/meshGeneratingFunctions.hh:170-183, :244-271).
+// ELLIPSOID_FROM_SPHERE (helper/meshGeneratingFunctions.hh:170-183, :244-271):
+// rotated unit icosphere, spherePointToEllipsoidPoint, the same rotation.
 Mesh ellipsoid_from_sphere(int min_triangles, double radius, double aspect) {
   Mesh m = merge_soup(icosphere_soup(min_triangles));
+  const Euler& R = shape_rotation();
   for (Vec3& p : m.v) {
+    p = R(p);
     double r2 = p.x * p.x + p.y * p.y;
     const int s = sgn(p.z);
     if (1 - r2 < 0) r2 = 1;
-    p = {p.x * radius, p.y * radius, s * aspect * radius * std::sqrt(1 - r2)};
+    p = R(Vec3{p.x * radius, p.y * radius, s * aspect * radius * std::sqrt(1 - r2)});
   }
   return m;
 }
@@ -344,24 +386,33 @@ std::string build_constants(TypeConstants& tc, int model, const std::vector<Vec3
   return "";
 }
 
-// rotateTriangularMeshXYZ (io/readPositionsBloodCells.cpp:39-118): the
-// matrix product Rz*Ry*Rx of the reference's column-first factors, applied
-// after centring on the bounding box (meshRotation :111-118, and the
-// bounding-box centring of :316-318).
+// loadParticles' placement of one cell (io/readPositionsBloodCells.cpp:290-361),
+// in the reference's order of operations: the template is translated by minus
+// its bounding-box centre (:316); meshRotation (:111-118) translates by minus
+// the centre of the new bounding box, applies rotateTriangularMeshXYZ
+// (:39-109: Rz * (Ry * Rx) of the column-first factors) and translates back;
+// positionCellInParticleField (:120-124) adds the starting point.
 void place_cell(const std::vector<Vec3>& rest, const double centre[3], const double ang[3],
                 std::vector<double>& out) {
-  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-  for (const Vec3& p : rest) {
-    const double q[3] = {p.x, p.y, p.z};
-    for (int a = 0; a < 3; ++a) {
-      lo[a] = std::min(lo[a], q[a]);
-      hi[a] = std::max(hi[a], q[a]);
-    }
-  }
-  const double c0[3] = {(lo[0] + hi[0]) / 2.0, (lo[1] + hi[1]) / 2.0, (lo[2] + hi[2]) / 2.0};
-  double A[3][3] = {{1, 0, 0}, {0, std::cos(ang[0]), std::sin(ang[0])}, {0, -std::sin(ang[0]), std::cos(ang[0])}};
-  double B[3][3] = {{std::cos(ang[1]), 0, -std::sin(ang[1])}, {0, 1, 0}, {std::sin(ang[1]), 0, std::cos(ang[1])}};
-  double Cz[3][3] = {{std::cos(ang[2]), std::sin(ang[2]), 0}, {-std::sin(ang[2]), std::cos(ang[2]), 0}, {0, 0, 1}};
+  auto bbox_mid = [](const std::vector<std::array<double, 3>>& v, double c[3], bool half_sum) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (const auto& q : v)
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = std::min(lo[a], q[a]);
+        hi[a] = std::max(hi[a], q[a]);
+      }
+    for (int a = 0; a < 3; ++a) c[a] = half_sum ? (hi[a] + lo[a]) * 0.5 : -(lo[a] + hi[a]) / 2.0;
+  };
+  std::vector<std::array<double, 3>> v(rest.size());
+  for (size_t i = 0; i < rest.size(); ++i) v[i] = {rest[i].x, rest[i].y, rest[i].z};
+  double t0[3], c2[3];
+  bbox_mid(v, t0, false);
+  for (auto& q : v)
+    for (int a = 0; a < 3; ++a) q[a] = q[a] + t0[a];
+  bbox_mid(v, c2, true);
+  const double A[3][3] = {{1, 0, 0}, {0, std::cos(ang[0]), std::sin(ang[0])}, {0, -std::sin(ang[0]), std::cos(ang[0])}};
+  const double B[3][3] = {{std::cos(ang[1]), 0, -std::sin(ang[1])}, {0, 1, 0}, {std::sin(ang[1]), 0, std::cos(ang[1])}};
+  const double Cz[3][3] = {{std::cos(ang[2]), std::sin(ang[2]), 0}, {-std::sin(ang[2]), std::cos(ang[2]), 0}, {0, 0, 1}};
   double BA[3][3], M[3][3];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
@@ -373,12 +424,12 @@ void place_cell(const std::vector<Vec3>& rest, const double centre[3], const dou
       M[i][j] = 0;
       for (int k = 0; k < 3; ++k) M[i][j] += Cz[i][k] * BA[k][j];
     }
-  for (const Vec3& p : rest) {
-    const double q[3] = {p.x - c0[0], p.y - c0[1], p.z - c0[2]};
+  for (const auto& p : v) {
+    const double q[3] = {p[0] + -c2[0], p[1] + -c2[1], p[2] + -c2[2]};
     for (int i = 0; i < 3; ++i) {
       double r = 0;
       for (int j = 0; j < 3; ++j) r += M[i][j] * q[j];
-      out.push_back(centre[i] + r);
+      out.push_back(centre[i] + (r + c2[i]));
     }
   }
 }

@@ -299,16 +299,26 @@ __global__ void __launch_bounds__(256) k_collide_stream_bulk(const LbmView<T> L,
   }
   if (failed && tid == 0) {
     atomicOr(L.status, STATUS_WAIT_TIMEOUT);
-    // let the copies already issued land before the CTA's shared memory is released
-    for (int q = k; q < issued; ++q)
-      if (!mbar_wait_bounded(&bars[q % P.stages], (uint32_t)((q / P.stages) & 1), P.spin_limit)) break;
+    // let the copies already issued land before the CTA's shared memory is
+    // released: each stage gets four more bounded waits.  A copy that has not
+    // landed even then leaves the handle unusable; STATUS_WAIT_TIMEOUT tells
+    // the host to discard it.
+    for (int q = k; q < issued; ++q) {
+      bool landed = false;
+      for (int tries = 0; tries < 4 && !landed; ++tries)
+        landed = mbar_wait_bounded(&bars[q % P.stages], (uint32_t)((q / P.stages) & 1), P.spin_limit);
+      if (!landed) break;
+    }
   }
 }
 
 template <typename T>
 bool make_bulk_plan(int nx, int ny, int nz, int stages, int ctas_target, BulkPlan* P) {
   if (nx <= 0 || ny <= 0 || nz <= 0 || stages < 2 || ctas_target < 1) return false;
-  if ((nx * sizeof(T)) % 16 != 0 || nx > 256) return false;
+  // cp.async.bulk wants 16-byte sizes and addresses: rows of populations and
+  // forces (nx T) and of the 32-bit node mask (nx words, so nx % 4 == 0; an
+  // FP64 lattice with nx = 2 mod 4 passes the first test but not this one)
+  if ((nx * sizeof(T)) % 16 != 0 || (nx * sizeof(uint32_t)) % 16 != 0 || nx > 256) return false;
   int R = 0;
   for (int r = 256 / nx; r >= 1; --r)
     if (ny % r == 0) {

@@ -13,6 +13,7 @@
 // calls whose launches may overlap (two host threads, or two streams with no
 // ordering between them) race on it and give wrong lists.  Calls issued one
 // after another on one stream, or otherwise ordered, are safe.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,7 +36,40 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
+// Per device: the id of the CUDA context the address was looked up in, and
+// the address.  Context ids are never reused within a process, so after a
+// cudaDeviceReset (which ends the context and unloads the library's device
+// image) the next call sees a new id and looks the address up again.
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
 int* g_scratch_ptr[kMaxDevices] = {};
+
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// The current context's id through the driver entry points the runtime
+// hands out (no link against libcuda); 0 when it cannot be had.
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 // Vertices whose tile lies outside [0, ntiles) are treated as unbinned (the
 // handle path marks those with -1), so no counter outside the scratch is hit.
@@ -55,8 +89,13 @@ __global__ void k_fill_checked(const int* vtile, int nvert, int ntiles, const in
   tile_vertices[offsets[t] + atomicAdd(cursor + t, 1)] = i;
 }
 
-// Looks up this device's scratch address once, on the first call made with
-// that device current; later calls on the device reuse the cached address.
+// Set-up: the device address of g_tile_scratch for the current device.  In
+// host code the array's name stands for a host-side shadow, not for device
+// memory, so the address must come from cudaGetSymbolAddress, called with
+// the device current.  It is looked up on the first call on each device (that
+// call also loads the library's device image there if it is not loaded yet)
+// and cached per device and context; a call in a new context of the device
+// looks it up again.
 int scratch_for_current_device(int** out, std::string& err) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -68,8 +107,11 @@ int scratch_for_current_device(int** out, std::string& err) {
     err = "device ordinal beyond the supported range";
     return HC_ERR_INVALID;
   }
+  // a thread whose context the runtime has not made current yet reads 0 and
+  // takes the lookup, which makes it current
+  unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || ctx == 0 || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_tile_scratch);
     if (e != cudaSuccess) {
@@ -77,6 +119,7 @@ int scratch_for_current_device(int** out, std::string& err) {
       return HC_ERR_CUDA;
     }
     g_scratch_ptr[dev] = static_cast<int*>(p);
+    g_scratch_ctx[dev] = current_context_id();
   }
   *out = g_scratch_ptr[dev];
   return HC_OK;

@@ -9,6 +9,7 @@ the library's message (the reference prints through hlog and exits).
 from __future__ import annotations
 
 import ctypes as C
+import math
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
@@ -120,6 +121,16 @@ def place_cells(mesh: Mesh, centres: np.ndarray, angles: np.ndarray) -> np.ndarr
     if rc != L.HC_OK:
         raise HemoCellError("placement failed")
     return out
+
+
+def pos_to_lattice(pos_um, angles_deg, dx: float):
+    """Lines of a .pos file (centre in micrometres, three angles in degrees) as
+    loadParticles reads them (io/readPositionsBloodCells.cpp:218-224, 327-351):
+    centres in lattice units, angles in radians and negated (the reference's
+    right- to left-handed conversion)."""
+    pos = np.asarray(pos_um, np.float64).reshape(-1, 3)
+    ang = np.asarray(angles_deg, np.float64).reshape(-1, 3)
+    return pos * (1e-6 / dx) + 0.0, (ang * (math.pi / 180.0)) * -1.0
 
 
 def pack_cells(dims, periodic, solid: Optional[np.ndarray], meshes: Sequence[Mesh], counts: Sequence[int],
@@ -250,6 +261,20 @@ class HemoCell:
         first = self._check(self._lib.hc_add_cells(self._h, type_id, centres.shape[0], _dp(centres), _dp(angles)))
         self.cell_types += [type_id] * centres.shape[0]
         return first
+
+    def loadParticles(self, type_id: int, pos_um, angles_deg) -> np.ndarray:
+        """HemoCell::loadParticles for one cell type from the rows of its
+        .pos file (centres in micrometres, angles in degrees): the cells the
+        reference admits (no vertex on a wall node or outside the lattice) are
+        added; returns the per-row mask of the cells added."""
+        centres, angles = pos_to_lattice(pos_um, angles_deg, self.dx)
+        centres = np.ascontiguousarray(centres, np.float64)
+        angles = np.ascontiguousarray(angles, np.float64)
+        mask = np.zeros(centres.shape[0], np.int32)
+        self._check(self._lib.hc_load_cells(self._h, type_id, centres.shape[0], _dp(centres), _dp(angles),
+                                            _ip(mask)))
+        self.cell_types += [type_id] * int(mask.sum())
+        return mask.astype(bool)
 
     def add_cells_xyz(self, type_id: int, xyz: np.ndarray) -> int:
         xyz = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)

@@ -123,6 +123,16 @@ int hc_add_cell_type(hc_handle* h, const char* name, int model, const hc_materia
  * rotateTriangularMeshXYZ(angles in rad) and translated to centres (lattice
  * units).  Returns the first new cell id. */
 int hc_add_cells(hc_handle* h, int type, int n, const double* centres, const double* angles);
+/* HemoCell::loadParticles with its admission of cells
+ * (io/readPositionsBloodCells.cpp:120-170, 354): places n cells as
+ * hc_add_cells does, but adds only the cells all of whose vertices the
+ * reference adds -- inside the lattice's box on every axis (periodic axes are
+ * not wrapped at loading) and with a nearest node int(x + 0.5) that is not a
+ * wall node; the other cells are left out, as deleteIncompleteCells removes
+ * them.
+ * loaded[n] (may be NULL) receives 1 for each cell added.  Returns the number
+ * of cells added (>= 0) or an HC_ERR_* code. */
+int hc_load_cells(hc_handle* h, int type, int n, const double* centres, const double* angles, int* loaded);
 /* place n cells from explicit vertex positions (n*nv*3, lattice units) */
 int hc_add_cells_xyz(hc_handle* h, int type, int n, const double* xyz);
 /* setMaterialTimeScaleSeparation / setParticleVelocityUpdateTimeScaleSeparation
@@ -216,7 +226,11 @@ int hc_read_neighbours(hc_handle* h, int* nb_offsets, int* nb_cells, int max_cel
  * streams) race on it and give wrong lists; calls ordered on one stream are
  * safe.  The first call on each device looks up that array's address (with
  * the device current), which may make the CUDA runtime load the library's
- * device code; make that first call before capturing any stream. */
+ * device code; make that first call before capturing any stream.  The
+ * address is kept per device and CUDA context: after a cudaDeviceReset the
+ * next call looks it up again, so a reset leaves no stale address behind.
+ * A tile of any size is sorted (up to 2048 vertices in shared memory, beyond
+ * that in place by a block-wide sorting network). */
 int hc_bin_tiles_noalloc(const int* vertex_tile, const int* vertex_cell, int nvert, int ntiles,
                          int* tile_offsets, int* tile_vertices, int* tile_cell_offsets, int* tile_cells,
                          int max_tile_cells, void* stream);
@@ -252,7 +266,8 @@ int hc_get_stats(hc_handle* h, hc_stats* out);  /* waits for the handle's stream
 int hc_vertex_count(const hc_handle* h);         /* vertices in use; does not wait */
 /* device status word, sticky: bit0 non-finite vertex velocity, bit1 cell
  * deleted at a wall, bit2 a shared-memory pipeline wait of the bulk-copy
- * collide-stream timed out (the step's results are then invalid), bit3 a
+ * collide-stream timed out (the step's results are then invalid and the
+ * handle must be destroyed: copies may still have been in flight), bit3 a
  * lattice node held more repulsion candidates than its slots (pairs were
  * dropped) */
 int hc_device_status(hc_handle* h, unsigned int* status);

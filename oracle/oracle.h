@@ -120,6 +120,33 @@ void orc_material_scale(int model, int nfaces, const double* units,
                         kCytoskeleton, coreRadius, radius (SI) */,
                         double* k_out /* 9 */);
 
+/* Cell geometry (geometry.cpp) ------------------------------------------- */
+/* constructSphereIcosahedron / constructRBCFromSphere /
+ * constructEllipsoidFromSphere (helper/meshGeneratingFunctions.hh:31-271):
+ * vertices xyz[nv][3] (lattice units) and outward faces tris[nf][3]; returns
+ * -1 when the buffers are too small (nv, nf still set) */
+int orc_mesh_icosphere(int min_triangles, double radius, double* xyz, int max_nv, int* tris, int max_nf, int* nv,
+                       int* nf);
+int orc_mesh_rbc(int min_triangles, double radius, double* xyz, int max_nv, int* tris, int max_nf, int* nv,
+                 int* nf);
+int orc_mesh_ellipsoid(int min_triangles, double radius, double aspect, double* xyz, int max_nv, int* tris,
+                       int max_nf, int* nv, int* nf);
+int orc_mesh_antipodal_pairs(const double* xyz, int nv, int* pairs, int max_pairs);
+/* loadParticles' placement (io/readPositionsBloodCells.cpp:39-124, 290-361):
+ * n cells of a template, centres in lattice units, angles in radians as the
+ * reference stores them (negated .pos angles); out[n][nv][3] */
+void orc_place_cells(const double* rest, int nv, int n, const double* centres, const double* angles, double* out);
+/* .pos lines (micrometres, degrees) to lattice-unit centres and the
+ * reference's radians (io/readPositionsBloodCells.cpp:218-224, 327-351) */
+void orc_pos_to_lattice(int n, const double* pos_um, const double* angles_deg, double dx, double* centres,
+                        double* angles);
+/* the project's seeded packer (no reference counterpart); returns the number
+ * of cells placed without overlap */
+int orc_pack_cells(int nx, int ny, int nz, const int* periodic, const uint8_t* solid, int ntypes,
+                   const double* const* rest, const int* nvs, const int* const* tris, const int* nfs,
+                   const int* counts, double margin, unsigned long long seed, int max_attempts, double* centres,
+                   double* angles, int* types);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,14 @@ _SIG = {
     "orc_type_constants": (None, [P, C.c_int, I, D, D, I, I, D, D, I, D]),
     "orc_units": (None, [C.c_double] * 6 + [D]),
     "orc_material_scale": (None, [C.c_int, C.c_int, D, C.c_double, C.c_double, D, D]),
+    "orc_mesh_icosphere": (C.c_int, [C.c_int, C.c_double, D, C.c_int, I, C.c_int, I, I]),
+    "orc_mesh_rbc": (C.c_int, [C.c_int, C.c_double, D, C.c_int, I, C.c_int, I, I]),
+    "orc_mesh_ellipsoid": (C.c_int, [C.c_int, C.c_double, C.c_double, D, C.c_int, I, C.c_int, I, I]),
+    "orc_mesh_antipodal_pairs": (C.c_int, [D, C.c_int, I, C.c_int]),
+    "orc_place_cells": (None, [D, C.c_int, C.c_int, D, D, D]),
+    "orc_pos_to_lattice": (None, [C.c_int, D, D, C.c_double, D, D]),
+    "orc_pack_cells": (C.c_int, [C.c_int, C.c_int, C.c_int, I, U8, C.c_int, C.POINTER(D), I, C.POINTER(I), I, I,
+                                 C.c_double, C.c_ulonglong, C.c_int, D, D, I]),
 }
 
 _lib = None
@@ -275,3 +283,108 @@ def apply_case(case, threads: int = 0, dx=0.5e-6, dt=1e-7, rho_p=1025.0, kBT=4.1
     for t, xyz in case.cells:
         o.add_cell(t, xyz)
     return o
+
+
+# ---------------------------------------------------------------------------
+# Cell geometry (oracle/geometry.cpp): the oracle's own mesh generators,
+# placement and packer.  ``geometry`` offers the functions a workload builder
+# needs (the same names and argument meaning as the product's), so a
+# hemocell_gb300.cases workload can be built without the product library.
+
+class Mesh:
+    """A closed triangle mesh: xyz (nv, 3) lattice units, tris (nf, 3)
+    outward oriented, inner (ni, 2) inner-link vertex pairs."""
+
+    def __init__(self, xyz, tris, inner=None):
+        self.xyz = xyz
+        self.tris = tris
+        self.inner = np.zeros((0, 2), np.int32) if inner is None else inner
+
+    @property
+    def nv(self) -> int:
+        return int(self.xyz.shape[0])
+
+    @property
+    def nf(self) -> int:
+        return int(self.tris.shape[0])
+
+
+def _mesh(fn, *args, min_triangles):
+    nf_cap = 20
+    while nf_cap < min_triangles:
+        nf_cap *= 4
+    nv_cap = nf_cap // 2 + 2
+    xyz = np.zeros((nv_cap, 3))
+    tris = np.zeros((nf_cap, 3), np.int32)
+    nv, nf = C.c_int(), C.c_int()
+    rc = fn(*args, _d(xyz), nv_cap, _i(tris), nf_cap, C.byref(nv), C.byref(nf))
+    if rc != 0:
+        raise RuntimeError("oracle mesh buffers too small")
+    return Mesh(xyz[: nv.value].copy(), tris[: nf.value].copy())
+
+
+class _Geometry:
+    """Workload geometry from the oracle alone (helper/meshGeneratingFunctions.hh,
+    io/readPositionsBloodCells.cpp, and the project's seeded packer)."""
+
+    @staticmethod
+    def icosphere(min_triangles: int, radius: float) -> Mesh:
+        return _mesh(lib().orc_mesh_icosphere, min_triangles, radius, min_triangles=min_triangles)
+
+    @staticmethod
+    def rbc_mesh(min_triangles: int, radius: float) -> Mesh:
+        return _mesh(lib().orc_mesh_rbc, min_triangles, radius, min_triangles=min_triangles)
+
+    @staticmethod
+    def ellipsoid_mesh(min_triangles: int, radius: float, aspect: float) -> Mesh:
+        return _mesh(lib().orc_mesh_ellipsoid, min_triangles, radius, aspect, min_triangles=min_triangles)
+
+    @staticmethod
+    def antipodal_pairs(xyz) -> np.ndarray:
+        xyz = np.ascontiguousarray(xyz, np.float64)
+        out = np.zeros((max(xyz.shape[0], 1), 2), np.int32)
+        n = lib().orc_mesh_antipodal_pairs(_d(xyz), xyz.shape[0], _i(out), out.shape[0])
+        if n < 0:
+            raise RuntimeError("antipodal pair buffer too small")
+        return out[:n].copy()
+
+    @staticmethod
+    def place_cells(mesh, centres, angles) -> np.ndarray:
+        centres = np.ascontiguousarray(centres, np.float64).reshape(-1, 3)
+        angles = np.ascontiguousarray(angles, np.float64).reshape(-1, 3)
+        n = centres.shape[0]
+        out = np.zeros((n * mesh.nv, 3))
+        lib().orc_place_cells(_d(np.ascontiguousarray(mesh.xyz, np.float64)), mesh.nv, n, _d(centres), _d(angles),
+                              _d(out))
+        return out
+
+    @staticmethod
+    def pos_to_lattice(pos_um, angles_deg, dx):
+        pos = np.ascontiguousarray(pos_um, np.float64).reshape(-1, 3)
+        ang = np.ascontiguousarray(angles_deg, np.float64).reshape(-1, 3)
+        c, a = np.zeros_like(pos), np.zeros_like(ang)
+        lib().orc_pos_to_lattice(pos.shape[0], _d(pos), _d(ang), float(dx), _d(c), _d(a))
+        return c, a
+
+    @staticmethod
+    def pack_cells(dims, periodic, solid, meshes, counts, margin, seed, max_attempts=20000):
+        nt = len(meshes)
+        total = int(sum(counts))
+        xyzs = [np.ascontiguousarray(m.xyz, np.float64) for m in meshes]
+        triss = [np.ascontiguousarray(m.tris, np.int32) for m in meshes]
+        xp = (D * nt)(*[_d(a) for a in xyzs])
+        tp = (I * nt)(*[_i(a) for a in triss])
+        nvs = np.array([m.nv for m in meshes], np.int32)
+        nfs = np.array([m.nf for m in meshes], np.int32)
+        cnt = np.array(counts, np.int32)
+        per = np.array(periodic, np.int32)
+        centres = np.zeros((max(total, 1), 3))
+        angles = np.zeros((max(total, 1), 3))
+        types = np.zeros(max(total, 1), np.int32)
+        sp = None if solid is None else np.ascontiguousarray(solid, np.uint8).ctypes.data_as(U8)
+        n = lib().orc_pack_cells(dims[0], dims[1], dims[2], _i(per), sp, nt, xp, _i(nvs), tp, _i(nfs), _i(cnt),
+                                 float(margin), C.c_ulonglong(seed), max_attempts, _d(centres), _d(angles), _i(types))
+        return centres[:n].copy(), angles[:n].copy(), types[:n].copy()
+
+
+geometry = _Geometry()

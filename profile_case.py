@@ -1,8 +1,8 @@
 """Run a named workload for a few steps, for profiling one kernel in isolation.
 
-    python -m hemocell_gb300.profile_case pipe --steps 10 --form f32
-    python -m hemocell_gb300.profile_case cube --n 128 --steps 10
-    python -m hemocell_gb300.profile_case pipe --graph-steps 20   # then 20 graph-replayed steps
+    python profile_case.py pipe --steps 10 --form f32
+    python profile_case.py cube --n 128 --steps 10
+    python profile_case.py pipe --graph-steps 20   # then 20 graph-replayed steps
 
 Workloads: ``pipe`` (64x64x256 cylinder at 25% haematocrit, 279 RBC),
 ``cube`` (periodic fluid box of edge n with a Kolmogorov force, no cells),
@@ -17,9 +17,13 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
+import sys
 
-from . import _lib as L
-from . import cases
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from hemocell_gb300 import _lib as L  # noqa: E402
+from hemocell_gb300 import cases  # noqa: E402
 
 
 def build_case(name: str, n: int):

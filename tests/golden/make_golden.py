@@ -7,11 +7,16 @@ are the pins: the oracle is checked against them on every CPU run
 (tests/test_gpu_golden.py).  Regenerate only when the restated algorithm
 changes on purpose:
 
-    python tests/golden/make_golden.py            # stage dumps + 50^3 shear, 1000 steps
+    python tests/golden/make_golden.py            # stage dumps, 50^3 shear (1000 steps), 64^3 suspension (300)
     python tests/golden/make_golden.py --pipe     # also the 64x64x256 pipe, 2000 steps (minutes)
 
-Every input comes from seeded builders in hemocell_gb300.cases, so only
-outputs are stored.
+Every input comes from the seeded builders in hemocell_gb300.cases, run
+with the oracle's own geometry (meshes, placement, packing: oracle/geometry.cpp),
+so no part of a fixture comes from the product library; only outputs are
+stored.  Large floating-point arrays are rounded to 40 mantissa bits (a
+relative change of at most 2^-41, about 5e-13) and stored byte-shuffled (the
+eight bytes of each double in eight planes) before compression, which keeps
+the full-field dumps of the larger runs to a few MB.
 """
 from __future__ import annotations
 
@@ -33,6 +38,40 @@ from oracle import oracle as orc  # noqa: E402
 STAGE_FILE = os.path.join(HERE, "stages_mixed_box.npz")
 SHEAR_FILE = os.path.join(HERE, "shear_rbc_50_1000.npz")
 PIPE_FILE = os.path.join(HERE, "pipe_ht25_2000.npz")
+SUSPENSION_FILE = os.path.join(HERE, "kolmogorov_64_300.npz")
+GEO = orc.geometry
+
+
+KEEP_BITS = 40   # mantissa bits kept in the large arrays: 2^-41 relative, far below the tolerances
+
+
+def save(path: str, d: dict) -> None:
+    """np.savez_compressed, with the float64 arrays of more than 64 values
+    rounded to KEEP_BITS mantissa bits and byte-shuffled."""
+    out = {}
+    drop = 52 - KEEP_BITS
+    for k, v in d.items():
+        v = np.asarray(v)
+        if v.dtype == np.float64 and v.size > 64:
+            bits = np.ascontiguousarray(v).reshape(-1).view(np.uint64)
+            bits = (bits + np.uint64(1 << (drop - 1))) & ~np.uint64((1 << drop) - 1)
+            out["shuffled__" + k] = np.ascontiguousarray(bits.view(np.uint8).reshape(-1, 8).T)
+            out["shape__" + k] = np.array(v.shape, np.int64)
+        else:
+            out[k] = v
+    np.savez_compressed(path, **out)
+
+
+def load(path: str) -> dict:
+    raw = np.load(path)
+    d = {}
+    for k in raw.files:
+        if k.startswith("shuffled__"):
+            name = k[len("shuffled__"):]
+            d[name] = np.ascontiguousarray(raw[k].T).view(np.float64).reshape(tuple(raw["shape__" + name]))
+        elif not k.startswith("shape__"):
+            d[k] = raw[k]
+    return d
 
 
 def sample_nodes(N: int, fluid: np.ndarray) -> np.ndarray:
@@ -45,7 +84,7 @@ def sample_nodes(N: int, fluid: np.ndarray) -> np.ndarray:
 def stage_dumps(threads: int = 0) -> dict:
     """Mixed box (one RBC, PLT and WBC, moving walls, uniform body force):
     three full steps, then each stage of a fourth step on its own."""
-    case = cases.mixed_box()
+    case = cases.mixed_box(geo=GEO)
     o = orc.apply_case(case, threads=threads)
     o.step(3)
     out = {}
@@ -70,18 +109,32 @@ def stage_dumps(threads: int = 0) -> dict:
 
 def shear_run(threads: int = 0) -> dict:
     """50^3 Couette box, one RBC (642 vertices), shear 100/s, 1000 steps."""
-    case = cases.shear_single_rbc(n=50, shear_rate=100.0, seed=1)
+    case = cases.shear_single_rbc(n=50, shear_rate=100.0, seed=1, geo=GEO)
     o = orc.apply_case(case, threads=threads)
     o.step(1000)
     return run_summary(case, o)
 
 
 def pipe_run(threads: int = 0) -> dict:
-    """64x64x256 pipe at 25% haematocrit (279 RBC), 2000 steps."""
-    case = cases.pipe_ht25(seed=1)
+    """64x64x256 pipe at 25% haematocrit (279 RBC), 2000 steps: the summary
+    plus every vertex position and velocity."""
+    case = cases.pipe_ht25(seed=1, geo=GEO)
     o = orc.apply_case(case, threads=threads)
     o.step(2000)
-    return run_summary(case, o, positions=False)
+    return run_summary(case, o)
+
+
+def suspension_case(geo=GEO):
+    """The 128^3 suspension's configuration at 64^3: periodic, Kolmogorov
+    forcing, RBC at 30% volume, PLT 1 per 10 RBC and one 2562-vertex WBC."""
+    return cases.kolmogorov_mix(n=64, rbc_fraction=0.30, n_wbc=1, plt_per_rbc=0.1, seed=2, geo=geo)
+
+
+def suspension_run(threads: int = 0) -> dict:
+    case = suspension_case()
+    o = orc.apply_case(case, threads=threads)
+    o.step(300)
+    return run_summary(case, o)
 
 
 def run_summary(case, o, positions: bool = True) -> dict:
@@ -120,14 +173,19 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     a = ap.parse_args()
     meta = {}
-    for name, fn, path in [("stages", stage_dumps, STAGE_FILE), ("shear", shear_run, SHEAR_FILE)] + (
+    meta_path = os.path.join(HERE, "generated_with.json")
+    if os.path.exists(meta_path):
+        with open(meta_path) as fh:
+            meta = json.load(fh).get("runs", {})
+    for name, fn, path in [("stages", stage_dumps, STAGE_FILE), ("shear", shear_run, SHEAR_FILE),
+                           ("suspension", suspension_run, SUSPENSION_FILE)] + (
             [("pipe", pipe_run, PIPE_FILE)] if a.pipe else []):
         t = time.time()
         d = fn(a.threads)
-        np.savez_compressed(path, **d)
+        save(path, d)
         meta[name] = {"file": os.path.basename(path), "seconds": round(time.time() - t, 1)}
         print(name, meta[name], {k: getattr(v, "shape", None) for k, v in d.items()})
-    with open(os.path.join(HERE, "generated_with.json"), "w") as fh:
+    with open(meta_path, "w") as fh:
         json.dump({"generator": "tests/golden/make_golden.py", "oracle": "oracle/oracle.cpp (FP64, "
                    "-ffp-contract=off)", "numpy": np.__version__, "runs": meta}, fh, indent=1)
 

@@ -1,5 +1,6 @@
 """The FP64 oracle against its committed golden dumps (tests/golden/), on the
-CPU: the stage-by-stage mixed box and the 50^3 sheared RBC after 1000 steps.
+CPU: the stage-by-stage mixed box and the 50^3 sheared RBC after 1000 steps
+(the larger runs, minutes of oracle time, are checked on the GPU only).
 Integer outputs (tile lists, cell ownership) must match exactly; floating
 point within 1e-12 relative L2 (the oracle is deterministic; the margin
 covers a last-bit difference of atan2 between the x86-64 and aarch64 C
@@ -25,9 +26,9 @@ def _gen():
 
 
 def check_against(got: dict, path: str, tol: float):
-    ref = np.load(path)
-    for k in ref.files:
-        a, b = np.asarray(got[k]), ref[k]
+    ref = _gen().load(path)
+    for k, b in ref.items():
+        a = np.asarray(got[k])
         assert a.shape == b.shape, k
         if np.issubdtype(b.dtype, np.integer):
             assert np.array_equal(a, b), k
@@ -46,5 +47,8 @@ def test_oracle_shear_rbc_1000_steps_match_golden(built):
 
 
 def test_golden_files_are_small():
+    """Small fixtures stay under 1 MB; the two full-field dumps (every vertex
+    position and velocity of the pipe and of the 64^3 suspension) under 8 MB."""
+    big = {"pipe_ht25_2000.npz", "kolmogorov_64_300.npz"}
     for f in os.listdir(GOLD):
-        assert os.path.getsize(os.path.join(GOLD, f)) < 1_000_000, f
+        assert os.path.getsize(os.path.join(GOLD, f)) < (8_000_000 if f in big else 1_000_000), f

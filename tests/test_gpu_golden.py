@@ -1,7 +1,11 @@
 """The GPU plain FP64 form against the oracle's golden dumps (tests/golden/):
-the 50^3 sheared RBC after 1000 steps and the 64x64x256 pipe with 279 RBC
-after 2000 steps.  Tile lists and cell ownership bit-exact; velocity,
-density, positions, centroids and volumes within relative L2 1e-10."""
+the 50^3 sheared RBC after 1000 steps, the 64x64x256 pipe with 279 RBC after
+2000 steps and the 64^3 Kolmogorov suspension of RBC, PLT and a WBC after
+300 steps.  Tile lists and cell ownership bit-exact; every vertex position
+and velocity, sampled and averaged fluid velocity and density, centroids and
+volumes within relative L2 1e-10.  The workloads are built with this
+library's geometry, which equals the oracle's bit for bit
+(tests/test_geometry_parity.py)."""
 import os
 
 import numpy as np
@@ -57,5 +61,17 @@ def test_gpu_pipe_2000_steps_match_golden(built, launch):
     case = cases.pipe_ht25(seed=1)
     hc = case.build(launch=launch)
     hc.iterate(2000)
-    check_against(_summary(case, hc, positions=False), g.PIPE_FILE, TOL)
+    check_against(_summary(case, hc), g.PIPE_FILE, TOL)
+    hc.close()
+
+
+@pytest.mark.parametrize("launch", [0, 1])
+def test_gpu_suspension_300_steps_match_golden(built, launch):
+    from hemocell_gb300 import cases
+    g = _gen()
+    case = g.suspension_case(geo=cases.PRODUCT)
+    assert {t for t, _ in case.cells} == {0, 1, 2}
+    hc = case.build(launch=launch)
+    hc.iterate(300)
+    check_against(_summary(case, hc), g.SUSPENSION_FILE, TOL)
     hc.close()

@@ -43,13 +43,17 @@ def test_mesh_counts_and_closure(built):
 
 
 def test_rbc_shape(built):
+    """The biconcave template after the shape constructor's fixed rotation
+    (pi/2, pi/2, 0): its axis lies along y, the disc spans x and z."""
     from hemocell_gb300 import cases, rbc_mesh
     m = rbc_mesh(600, 7.82)
-    r = np.hypot(m.xyz[:, 0], m.xyz[:, 1])
+    r = np.hypot(m.xyz[:, 0], m.xyz[:, 2])
     assert abs(r.max() - 7.82) < 1e-9
-    assert 2.2 < m.xyz[:, 2].max() < 2.4   # Evans-Fung maximum half thickness ~0.29 R
+    assert 2.2 < m.xyz[:, 1].max() < 2.4   # Evans-Fung maximum half thickness ~0.29 R
+    # the continuous Evans-Fung shape of R = 3.91 um encloses 81.76 um^3; the
+    # 1280-face mesh a little less
     vol_um3 = cases.mesh_volume(m) * 0.5 ** 3
-    assert 75 < vol_um3 < 95
+    assert 80.5 < vol_um3 < 81.76
 
 
 def test_antipodal_pairs(built):
@@ -75,6 +79,17 @@ def test_placement_matches_reference_rotation(built):
     c0 = (m.xyz.min(axis=0) + m.xyz.max(axis=0)) / 2
     expect = (m.xyz - c0) @ M.T + cen
     assert np.allclose(got, expect, atol=1e-12)
+
+
+def test_stretch_cell_disc_lies_in_the_xy_plane(built):
+    """stretch_RBC.pos places the cell with angles (90, 0, 0): the template's
+    y axis turns onto z, so the disc spans x and y as the validation measures
+    its axial (x) and transverse (y) diameters."""
+    from hemocell_gb300 import cases
+    xyz = cases.stretch_cell(320).cells[0][1]
+    ext = np.ptp(xyz, axis=0) * 0.5          # micrometres
+    assert abs(ext[0] - 7.82) < 1e-6 and abs(ext[1] - 7.82) < 1e-6
+    assert ext[2] < 2.7
 
 
 def test_packing_seeded_and_disjoint(built):

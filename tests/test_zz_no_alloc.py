@@ -111,3 +111,36 @@ def test_noalloc_rejects_sizes_beyond_the_fixed_maximum(built):
     assert b"131072" in lib.hc_last_error(None)
     rc = lib.hc_bin_tiles_noalloc(p, p, 4, 0, p, p, p, p, 4, None)
     assert rc == L.HC_ERR_INVALID
+
+
+def test_noalloc_crowded_tile_and_many_tiles(built):
+    """More tiles than one scan block (5000 > 1024) and one tile holding 6000
+    vertices (beyond the 2048 the shared-memory sort holds), against a numpy
+    restatement of the lists: vertices ascending per tile, distinct cells per
+    tile ascending (vertex ids grow with the cell id).  Called twice with
+    different contents, as a second call also shows the counters cleared."""
+    torch = pytest.importorskip("torch")
+    from hemocell_gb300 import _lib as L
+    lib = L.lib()
+    dev = torch.device("cuda", 0)
+    nt, V = 5000, 40000
+    vcell_h = (np.arange(V) // 642).astype(np.int32)
+    vcell = torch.from_numpy(vcell_h).to(dev)
+    rng = np.random.default_rng(17)
+    for call in range(2):
+        vt = rng.integers(0, nt, V).astype(np.int32)
+        crowd = rng.choice(V, 6000, replace=False)
+        vt[crowd] = 17 + call
+        vt[rng.choice(V, 50, replace=False)] = -1            # unbinned
+        got = _call(lib, torch, torch.from_numpy(vt).to(dev), vcell, nt, V)
+        keep = np.flatnonzero(vt >= 0)
+        counts = np.bincount(vt[keep], minlength=nt)
+        assert counts[17 + call] > 2048
+        offs = np.concatenate([[0], np.cumsum(counts)])
+        assert np.array_equal(got["tile_offsets"], offs)
+        order = keep[np.lexsort((keep, vt[keep]))]
+        assert np.array_equal(got["tile_vertices"][: keep.size], order)
+        cells = [np.unique(vcell_h[order[offs[t]:offs[t + 1]]]) for t in range(nt)]
+        coffs = np.concatenate([[0], np.cumsum([c.size for c in cells])])
+        assert np.array_equal(got["tile_cell_offsets"], coffs)
+        assert np.array_equal(got["tile_cells"][: coffs[-1]], np.concatenate(cells))
