@@ -30,6 +30,7 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import argparse
 import json
+import math
 import statistics
 import subprocess
 import sys
@@ -359,45 +360,82 @@ def timescale_leg(steps: int, warmup: int):
             "value": case.N * n / (ms * 1e3), "unit": "MLUPS", "ms_per_step": ms / n, "status": status}
 
 
-def serving_leg(args):
-    """Continuous batching of the stream of independent sheared-box solves
-    (box edge 32-96, 1-8 RBC, 500-5000 steps, Poisson arrivals at 200/s):
-    solves/s and latency of the batched server in FP32 and FP64, against the
-    same requests run one at a time in the plain FP64 form."""
+def small_box_kernels():
+    """Per-kernel device times of one small solve (32^3 box, one RBC) in the
+    three forms: why batching raises FP64 throughput less than FP32's."""
+    from hemocell_gb300 import _lib as L
+    from hemocell_gb300 import serving as S
+    r = S.Request(id=0, arrival=0.0, n=32, n_rbc=1, shear_rate=200.0, stiffness=1.0, steps=500, seed=7)
+    s = S.Solve(r)
+    out = {"box": "32^3 sheared box, one RBC (642 vertices)", "nodes": 32 ** 3}
+    for name, form in (("f32_batched", L.HC_FORM_MIXED_F32), ("f64_batched", L.HC_FORM_PLAIN_F64)):
+        hc = s.build(form, L.HC_LAUNCH_BATCHED)
+        hc.iterate(10)
+        out[name + "_kernels_ms"] = hc.profile_kernels(100)
+        hc.close()
+    hc = s.build(L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_PER_STAGE)
+    hc.iterate(10)
+    out["f64_per_stage_ms_per_step"] = hc.time_steps(100) / 100
+    hc.close()
+    return out
+
+
+def serving_leg(args, fp64_pipe_mlups=None):
+    """Continuous batching of the streams of independent sheared-box solves
+    (box edge 32-96, 1-8 RBC, 500-5000 steps, Poisson arrivals at 200/s),
+    seeds 1, 2 and 3: per seed, the same requests served one at a time in the
+    plain FP64 form, and batched in FP32 and in FP64; then the seed-1 stream
+    saturated (FP32) and at half the measured capacity."""
     import torch
     from hemocell_gb300 import _lib as L
     from hemocell_gb300 import serving as S
-    stream = S.request_stream(seed=1, rate=200.0, count=10000)
     free, _ = torch.cuda.mem_get_info()
     budget = int(min(0.5 * free, 64 << 30))
-    head = stream[:args.serve_requests]
-    few = stream[:args.serve_solo]
-    solves = {r.id: S.Solve(r) for r in head}        # geometry and packing, outside the clock
-    kw = dict(budget_bytes=budget, max_slots=64, chunk_steps=50, solves=solves)
 
     def trim(d):
         return {k: v for k, v in d.items() if k != "results"}
 
-    solo = S.solo(few, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_PER_STAGE, solves=solves)
-    few32 = S.serve(few, L.HC_FORM_MIXED_F32, **kw)
-    few64 = S.serve(few, L.HC_FORM_PLAIN_F64, **kw)
+    per_seed = {}
+    for seed in (1, 2, 3):
+        stream = S.request_stream(seed=seed, rate=200.0, count=10000)
+        reqs = stream[:args.serve_solo]
+        solves = {r.id: S.Solve(r) for r in reqs}        # geometry and packing, outside the clock
+        kw = dict(budget_bytes=budget, max_slots=64, chunk_steps=50, solves=solves)
+        solo = S.solo(reqs, L.HC_FORM_PLAIN_F64, L.HC_LAUNCH_PER_STAGE, solves=solves)
+        b32 = S.serve(reqs, L.HC_FORM_MIXED_F32, **kw)
+        b64 = S.serve(reqs, L.HC_FORM_PLAIN_F64, **kw)
+        per_seed[str(seed)] = {"requests": len(reqs), "solo_plain_f64": trim(solo), "batched_f32": trim(b32),
+                               "batched_f64": trim(b64),
+                               "speedup_f32_vs_solo": b32["solves_per_s"] / solo["solves_per_s"],
+                               "speedup_f64_vs_solo": b64["solves_per_s"] / solo["solves_per_s"]}
+    stream = S.request_stream(seed=1, rate=200.0, count=10000)
+    head = stream[:args.serve_requests]
+    solves = {r.id: S.Solve(r) for r in head}
+    kw = dict(budget_bytes=budget, max_slots=64, chunk_steps=50, solves=solves)
     sat32 = S.serve(head, L.HC_FORM_MIXED_F32, **kw)
-    # below saturation: the same requests at half the measured FP32 capacity
     rate_sub = 0.5 * sat32["solves_per_s"]
     sub = S.with_arrivals(head[: max(8, args.serve_requests // 3)], rate_sub, seed=2)
     sub32 = S.serve(sub, L.HC_FORM_MIXED_F32, **kw)
-    return {
+    small = small_box_kernels()
+    geo = lambda k: math.exp(sum(math.log(per_seed[s][k]) for s in per_seed) / len(per_seed))
+    out = {
         "workload": "independent sheared boxes, edge U{32,48,64,96}, 1-8 RBC (642 vertices), shear 50-500/s, "
-                    "kLink/kBend x log-U(0.5,5), 500-5000 steps; Poisson arrivals, seed 1",
+                    "kLink/kBend x log-U(0.5,5), 500-5000 steps; Poisson arrivals at 200/s",
         "budget_bytes": budget, "max_slots": 64, "chunk_steps": 50,
-        "solo_plain_f64": trim(solo),
-        "batched_f32_same_requests": trim(few32),
-        "batched_f64_same_requests": trim(few64),
-        "speedup_f32_vs_solo": few32["solves_per_s"] / solo["solves_per_s"],
-        "speedup_f64_vs_solo": few64["solves_per_s"] / solo["solves_per_s"],
+        "per_seed": per_seed,
+        "speedup_f32_vs_solo_geomean": geo("speedup_f32_vs_solo"),
+        "speedup_f64_vs_solo_geomean": geo("speedup_f64_vs_solo"),
         "saturated_f32_200_per_s": trim(sat32),
         "subsaturated_f32": dict(trim(sub32), offered_rate_target=rate_sub),
+        "small_box": small,
     }
+    if fp64_pipe_mlups:
+        # the FP64 arithmetic bound: the pipe's FP64 form keeps the FP64 pipe
+        # busy, so no mix of solves steps FP64 lattices much faster than that
+        solo_mlups = [per_seed[s]["solo_plain_f64"]["mlups"] for s in per_seed]
+        out["fp64_note"] = {"fp64_pipe_mlups": fp64_pipe_mlups, "solo_plain_f64_mlups": solo_mlups,
+                            "ceiling_over_solo": [fp64_pipe_mlups / m for m in solo_mlups]}
+    return out
 
 
 def pipe_config(case, nvertices: int) -> dict:
@@ -545,7 +583,7 @@ def main():
     if not args.no_kolmogorov:
         extra["kolmogorov"] = kolmogorov_leg(min(args.steps, 1000), args.warmup, tune_cache)
     if not args.no_serving:
-        extra["serving"] = serving_leg(args)
+        extra["serving"] = serving_leg(args, extra.get("fp64_batched", {}).get("value"))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -1084,6 +1084,11 @@ int autotune(hc_handle* h, const char* cache) {
   if (h->frep_wall) parts.push_back({h->frep_wall, 3 * h->ts * (size_t)h->rep_vcap});
   parts.push_back({h->status, sizeof(unsigned int)});
   parts.push_back({h->stamp, sizeof(uint32_t)});
+  // the node tags: a spread already fused into the next force field has
+  // tagged its stencil nodes, and the tagged node-velocity forms evaluate
+  // only nodes whose tag equals the step stamp; the trial steps overwrite
+  // tags with later stamps
+  parts.push_back({h->ntag, sizeof(uint32_t) * (size_t)h->N});
   size_t total = 0;
   for (auto& pr : parts) total += (pr.second + 255) / 256 * 256;
   char* snap = nullptr;

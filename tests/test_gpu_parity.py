@@ -552,13 +552,18 @@ def test_programmatic_dependent_launch_same_results(built, form):
                                        ((64, 2), 0x2000), ((256, 1), 1 | 0x3000), ((128, 1), 1 | 0x2000)])
 @pytest.mark.parametrize("walls", ["moving", "static", "odd"])
 def test_collide_stream_variants_same_bits(built, form, shape, var, walls):
-    """The direct collide-stream variants compute the same bits as the
-    whole-row kernel, over graph-replayed steps with cells: the interior pull
-    (tune[7] bit 12), evict-last population stores (bit 13), warps shaped as
-    8 x 4 and 16 x 2 tiles, one thread per fluid node (kind 1) with the interior
-    pull and evict-last stores, with moving walls (a sheared box with the moving-wall
-    term), with walls at rest (a small pipe, the term compiled out) and on a
-    21 x 17 x 19 lattice (no size a multiple of a block or column length)."""
+    """The direct collide-stream variants against the whole-row kernel: the
+    interior pull (tune[7] bit 12), evict-last population stores (bit 13),
+    warps shaped as 8 x 4 and 16 x 2 tiles, one thread per fluid node (kind 1)
+    with the interior pull and evict-last stores, with moving walls (a sheared
+    box with the moving-wall term), with walls at rest (a small pipe, the term
+    compiled out) and on a 21 x 17 x 19 lattice (no size a multiple of a block
+    or column length).  One collide-stream stage from the same random state
+    gives the same bits; 30 graph-replayed steps with cells agree within the
+    run tolerance (FP64 1e-12, FP32 1e-5) and delete the same cells: the
+    spread's float atomics add the vertices of a node in whatever order they
+    arrive, so two runs need not agree to the last bit once several vertices
+    share a node."""
     from hemocell_gb300 import _lib as L
     C = _cases()
     if walls == "moving":
@@ -572,20 +577,37 @@ def test_collide_stream_variants_same_bits(built, form, shape, var, walls):
         xyz = C.place_cells(t.mesh, np.array([[20.6, 8.0, 9.0]]), np.array([[0.4, -0.3, 0.2]]))
         case = C.Case("odd", n, (1, 1, 0), flags=flags, walls=wl, types=[t], cells=[(0, xyz)],
                       body_mode=L.HC_BODY_UNIFORM, body=(3e-6, -2e-6, 0.0))
-    a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
-    b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
-    t = a.tuning()
-    t[0], t[1] = 0, 1
-    t[7] &= ~0xf0ff
-    a.set_tuning(t)
-    t[0], t[1] = shape
-    t[7] |= var
-    b.set_tuning(t)
-    assert b.tuning()[7] & 0xf0ff == var
+
+    def pair():
+        a = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+        b = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+        t = a.tuning()
+        t[0], t[1] = 0, 1
+        t[7] &= ~0xf0ff
+        a.set_tuning(t)
+        t[0], t[1] = shape
+        t[7] |= var
+        b.set_tuning(t)
+        assert b.tuning()[7] & 0xf0ff == var
+        return a, b
+
+    a, b = pair()
+    randomize(case, a, _orc().apply_case(case))
+    randomize(case, b, _orc().apply_case(case))
+    a.stage(1)
+    b.stage(1)
+    assert np.array_equal(b.read_populations(), a.read_populations())
+    assert np.array_equal(b.read_force_field(0), a.read_force_field(0))
+    a.close()
+    b.close()
+    a, b = pair()
     a.iterate(30)
     b.iterate(30)
-    assert np.array_equal(b.read_vertices()[0], a.read_vertices()[0])
-    assert np.array_equal(b.read_fluid()[1], a.read_fluid()[1])
+    tol = 1e-12 if form == 0 else 1e-5
+    fluid = case.flags_array() == 0
+    assert rel_l2(b.read_vertices()[0], a.read_vertices()[0]) < tol
+    assert rel_l2(b.read_fluid()[1][:, fluid], a.read_fluid()[1][:, fluid]) < tol
+    assert np.array_equal(b.read_cells()[0], a.read_cells()[0])
     assert b.device_status() == a.device_status()
     a.close()
     b.close()
