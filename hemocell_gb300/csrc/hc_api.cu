@@ -276,6 +276,24 @@ void invalidate_graph(hc_handle* h) {
   h->graph_valid = false;
 }
 
+// Whether the node-velocity form of a tuning reads the node tags: every form
+// but the dense one (every fluid node in whole warps), which needs 32-bit
+// indices.  Without tags the spreads skip their tag stores, eight scattered
+// 4-byte stores per vertex.
+bool tags_needed(const hc_handle* h, const int* tune) {
+  return !((tune[7] & 0x300) == 0x300 && 19LL * h->N < (1LL << 31));
+}
+
+int undo_fused_spread(hc_handle* h);
+
+// A new tuning whose node velocity reads tags, while the spread already fused
+// into the next force field wrote none: undo it, so that the next step
+// spreads (and tags) afresh.
+int retag_if_needed(hc_handle* h, const int* old_tune) {
+  if (tags_needed(h, h->tune) && !tags_needed(h, old_tune)) return undo_fused_spread(h);
+  return HC_OK;
+}
+
 template <typename T>
 LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   LbmView<T> L;
@@ -291,7 +309,7 @@ LbmView<T> lbm_view(hc_handle* h, int src, int fcur) {
   L.nbmask = h->nbmask;
   L.flag = h->flag;
   L.bodyz = (const T*)h->bodyz;
-  L.ntag = h->ntag;
+  L.ntag = tags_needed(h, h->tune) ? h->ntag : nullptr;
   L.unode = (T*)h->unode;
   L.stamp = h->stamp;
   L.reverse = src;  // alternates with the buffer parity
@@ -1062,10 +1080,12 @@ int autotune(hc_handle* h, const char* cache) {
     int t[8];
     while (in >> k >> t[0] >> t[1] >> t[2] >> t[3] >> t[4] >> t[5] >> t[6] >> t[7])
       if (k == key) {
+        int old_tune[8];
+        std::memcpy(old_tune, h->tune, sizeof(old_tune));
         std::memcpy(h->tune, t, sizeof(t));
         if (!set_bulk_plan<T>(h, h->tune[7])) h->tune[7] = 0;
         invalidate_graph(h);
-        return HC_OK;
+        return retag_if_needed(h, old_tune);
       }
   }
   // Every candidate runs real steps (no graph) from the same device snapshot
@@ -1110,6 +1130,8 @@ int autotune(hc_handle* h, const char* cache) {
   }
   const int cur0 = h->cur, iter0 = h->iter;
   const bool sd0 = h->spread_done, sa0 = h->stamp_ahead;
+  int tune0[8];
+  std::memcpy(tune0, h->tune, sizeof(tune0));
   auto restore = [&]() -> int {
     size_t off = 0;
     for (auto& pr : parts) {
@@ -1274,6 +1296,7 @@ int autotune(hc_handle* h, const char* cache) {
   snap = nullptr;
   if (rc != HC_OK) return rc;
   invalidate_graph(h);
+  if ((rc = retag_if_needed(h, tune0)) != HC_OK) return rc;
   if (cache && *cache) {
     std::ofstream out(cache, std::ios::app);
     out << key;
@@ -2254,9 +2277,11 @@ int hc_set_tuning(hc_handle* h, const int* in8) {
       if (!ok) return fail(h, HC_ERR_INVALID, "the lattice does not allow the bulk collide-stream (row bytes, rows, shared memory)");
     }
   }
+  int old_tune[8];
+  std::memcpy(old_tune, h->tune, sizeof(old_tune));
   std::memcpy(h->tune, in8, sizeof(h->tune));
   invalidate_graph(h);
-  return HC_OK;
+  return retag_if_needed(h, old_tune);
 }
 
 // ---- cell information and CSV output --------------------------------------

@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256) k_spread(const LbmView<T> L, const Vertex
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     if (K.node[j] < 0) continue;
-    L.ntag[K.node[j]] = stamp;
+    if (L.ntag) L.ntag[K.node[j]] = stamp;
     FieldLayout<T>::add(F, L.N, K.node[j], fx * K.w[j], fy * K.w[j], fz * K.w[j]);
   }
   pdl_trigger();
@@ -375,7 +375,7 @@ __global__ void k_mark_nodes(const LbmView<T> L, const VertexView<T> vv) {
   ibm_weights(L, vv.x[i], vv.x[vv.V + i], vv.x[2 * vv.V + i], K);
 #pragma unroll
   for (int j = 0; j < 8; ++j)
-    if (K.node[j] >= 0) L.ntag[K.node[j]] = stamp;
+    if (K.node[j] >= 0 && L.ntag) L.ntag[K.node[j]] = stamp;
 }
 template <typename T>
 cudaError_t launch_mark_nodes(const LbmView<T>& L, const VertexView<T>& vv, cudaStream_t s) {
@@ -699,7 +699,7 @@ __device__ __forceinline__ void spread_vertex(const MechView<T>& M, int gi, V3t<
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     if (K.node[j] < 0) continue;
-    M.L.ntag[K.node[j]] = stamp;
+    if (M.L.ntag) M.L.ntag[K.node[j]] = stamp;
     FieldLayout<T>::add(F, M.L.N, K.node[j], f.x * K.w[j], f.y * K.w[j], f.z * K.w[j]);
   }
 }

@@ -33,7 +33,9 @@ struct LbmView {
   const uint32_t* __restrict__ nbmask;
   const uint8_t* __restrict__ flag;
   const T* __restrict__ bodyz;  // [3][nz]
-  uint32_t* ntag;                // per node: stamp of the last step whose stencils touch it
+  uint32_t* ntag;                // per node: stamp of the last step whose stencils touch it; null
+                                 // when the node-velocity form in use evaluates every fluid node
+                                 // (the spreads then write no tags)
   T* unode;                      // [3][N] velocity of tagged nodes
   uint32_t* stamp;               // device step stamp (advanced by interp_advance)
   int reverse;                   // sweep the lattice from the last z-plane down

@@ -896,3 +896,34 @@ def test_fused_advance_same_results(built, form):
     assert np.array_equal(a[3], b[3]) and a[5] == b[5]
     for k in ("vertex_node", "tile_offsets", "tile_cells"):
         assert np.array_equal(a[4][k], b[4][k]), k
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_node_tags_skipped_with_dense_node_velocity(built, form):
+    """With the dense node velocity (tune[7] bits 8-9 = 3) the spreads write no
+    node tags.  Switching to a tagged form in mid-run, while the next step's
+    spread is already fused into the force field, spreads again with tags:
+    every run matches the FP64 oracle at the form's run tolerance."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_periodic()
+    o = _orc().apply_case(case)
+    runs = {}
+    for name, first, second in (("dense", 0x300, 0x300), ("dense_then_tagged", 0x300, 0x000),
+                                ("tagged_then_dense", 0x000, 0x300)):
+        hc = case.build(form=form, launch=L.HC_LAUNCH_BATCHED)
+        t = hc.tuning()
+        t[7] = (t[7] & ~0x300) | first
+        hc.set_tuning(t)
+        hc.iterate(12)
+        t[7] = (t[7] & ~0x300) | second
+        hc.set_tuning(t)
+        hc.iterate(13)
+        runs[name] = (hc.read_vertices()[0], hc.read_fluid()[1], hc.device_status())
+        hc.close()
+    o.step(25)
+    xo, uo = o.read_vertices()[0], o.read_fluid()[1]
+    tol = RUN_TOL if form == 0 else 1e-4
+    for name, (x, u, st) in runs.items():
+        assert rel_l2(x, xo) < tol, name
+        assert rel_l2(u, uo) < tol, name
+        assert st & 5 == 0, name
