@@ -9,7 +9,10 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libhcgpu.so")
+# HEMOCELL_GB300_CHECKED=1 loads the bounds-checked build (hemocell_gb300.build
+# build(checked=True)) in place of the product library
+LIB_PATH = os.path.join(HERE, "libhcgpu_checked.so" if os.environ.get("HEMOCELL_GB300_CHECKED") == "1"
+                        else "libhcgpu.so")
 
 HC_OK = 0
 HC_ERR_INVALID = -1

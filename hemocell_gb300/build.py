@@ -17,6 +17,11 @@ ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhcgpu.so")
+# the bounds-checked build (-DHC_CHECKED): every guarded index is compared with
+# its array's length before the access and a violation sets a status bit
+# instead of faulting; built on demand by build(checked=True)
+BUILD_CHECKED = os.path.join(BUILD, "checked")
+LIB_CHECKED = os.path.join(HERE, "libhcgpu_checked.so")
 
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 UNITS = ["hc_lattice.cu", "hc_cells.cu", "hc_api.cu", "hc_noalloc.cu", "hc_batch.cu", "hc_host.cpp"]
@@ -33,13 +38,13 @@ def _headers_mtime() -> float:
     return max(os.path.getmtime(p) for p in paths)
 
 
-def _compile(unit: str, hdr_mtime: float, verbose: bool) -> str:
+def _compile(unit: str, hdr_mtime: float, verbose: bool, checked: bool = False) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit + ".o")
+    obj = os.path.join(BUILD_CHECKED if checked else BUILD, unit + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), hdr_mtime):
         return obj
     cmd = [_nvcc(), GENCODE, "-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
-           "-I", CSRC, "-c", src, "-o", obj]
+           "-I", CSRC, "-c", src, "-o", obj] + (["-DHC_CHECKED"] if checked else [])
     if unit.endswith(".cpp"):
         # host geometry without fused multiply-adds: the same doubles on x86-64
         # and aarch64, and the same as the FP64 CPU restatement's
@@ -77,20 +82,23 @@ def _cuda_home() -> str:
     return os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
-def build(verbose: bool = False) -> str:
-    """Compile every unit and link libhcgpu.so; returns the library path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, checked: bool = False) -> str:
+    """Compile every unit and link libhcgpu.so (with checked=True the
+    bounds-checked libhcgpu_checked.so instead); returns the library path."""
+    os.makedirs(BUILD_CHECKED if checked else BUILD, exist_ok=True)
+    lib = LIB_CHECKED if checked else LIB
     hdr = _headers_mtime()
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda u: _compile(u, hdr, verbose), UNITS))
+        objs = list(ex.map(lambda u: _compile(u, hdr, verbose, checked), UNITS))
     newest = max(os.path.getmtime(o) for o in objs)
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
-        cmd = [_nvcc(), GENCODE, "-shared", "-o", LIB] + objs + ["-lcudart"]
+    if not os.path.exists(lib) or os.path.getmtime(lib) < newest:
+        cmd = [_nvcc(), GENCODE, "-shared", "-o", lib] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    build_examples(verbose)
-    return LIB
+    if not checked:
+        build_examples(verbose)
+    return lib
 
 
 if __name__ == "__main__":

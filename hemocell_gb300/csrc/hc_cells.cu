@@ -82,7 +82,7 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
     if (w == T(0)) continue;
     const long long nd =
         (long long)idx[0][ax] + (long long)L.nx * ((long long)idx[1][ay] + (long long)L.ny * idx[2][az]);
-    if (L.flag[nd] != 0) continue;
+    if (!HC_IN(L.status, nd, L.N) || L.flag[nd] != 0) continue;
     total += w;
     K.node[s] = nd;
     K.w[s] = w;
@@ -797,6 +797,7 @@ __device__ __forceinline__ void gather_cell(const MechView<T>& M, const TypeDev&
   const int voff = M.cell_voff[cell];
   T* sbf = sx + 3 * nv;  // own bending force per vertex
   uint8_t* srn = reinterpret_cast<uint8_t*>(sbf + 3 * nv);  // valence per vertex
+  if (!HC_IN(vv.status, (long long)voff + nv - 1, V)) return;  // the cell's vertices in the arrays
   const bool alive = vv.alive[cell] != 0;
   for (int k = tid; k < nv; k += bs) srn[k] = (uint8_t)t.ring_n[k];
   // positions relative to the cell's vertex 0 (translation invariant forces;

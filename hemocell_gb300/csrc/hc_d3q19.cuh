@@ -142,7 +142,8 @@ __device__ __forceinline__ uint32_t wall_class(const LbmView<T>& L, int i, int X
   const int ox = cxi(i) < 0 ? nb.xm : (cxi(i) > 0 ? nb.xp : X);
   const int oy = cyi(i) < 0 ? nb.ym : (cyi(i) > 0 ? nb.yp : Y);
   const int oz = czi(i) < 0 ? nb.zm : (czi(i) > 0 ? nb.zp : Z);
-  uint32_t c = L.flag[(long long)ox + (long long)L.nx * ((long long)oy + (long long)L.ny * oz)];
+  const long long on = (long long)ox + (long long)L.nx * ((long long)oy + (long long)L.ny * oz);
+  uint32_t c = HC_IN(L.status, on, L.N) ? L.flag[on] : 0u;
   return c < (uint32_t)MAX_WALL_CLASSES ? c : 0u;
 }
 
@@ -154,19 +155,20 @@ __device__ __forceinline__ void pull(const LbmView<T>& L, const T* __restrict__ 
   const long long N = L.N;
   const Nbr nb(X, Y, Z, L.nx, L.ny, L.nz);
   const uint32_t cls = m >> NB_CLASS_SHIFT;
-  f[0] = src[n];
+  f[0] = HC_IN(L.status, n, N) ? src[n] : T(0);
 #pragma unroll
   for (int j = 1; j < 19; ++j) {
     const int i = oppi(j);  // x - c_j == x + c_i
     if (m & (1u << (i - 1))) {
       const uint32_t c = wall_class(L, i, X, Y, Z, nb, cls);
       const T cuw = T(cxi(i)) * L.uw[c][0] + T(cyi(i)) * L.uw[c][1] + T(czi(i)) * L.uw[c][2];
-      f[j] = src[i * N + n] - T(6.0 * wi(i)) * cuw;
+      f[j] = (HC_IN(L.status, i * N + n, 19 * N) ? src[i * N + n] : T(0)) - T(6.0 * wi(i)) * cuw;
     } else {
       const int sx = cxi(j) > 0 ? nb.xm : (cxi(j) < 0 ? nb.xp : X);
       const int sy = cyi(j) > 0 ? nb.ym : (cyi(j) < 0 ? nb.yp : Y);
       const int sz = czi(j) > 0 ? nb.zm : (czi(j) < 0 ? nb.zp : Z);
-      f[j] = src[j * N + ((long long)sx + (long long)L.nx * ((long long)sy + (long long)L.ny * sz))];
+      const long long k = j * N + ((long long)sx + (long long)L.nx * ((long long)sy + (long long)L.ny * sz));
+      f[j] = HC_IN(L.status, k, 19 * N) ? src[k] : T(0);
     }
   }
 }
@@ -203,14 +205,15 @@ __device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __rest
     uy = L.uw[cls][1];
     uz = L.uw[cls][2];
   }
-  f[0] = __ldg(src + n);
+  f[0] = HC_IN(L.status, n, N) ? __ldg(src + n) : T(0);
 #pragma unroll
   for (int j = 1; j < 19; ++j) {
     const int i = oppi(j);  // x - c_j == x + c_i
     const bool bb = (m >> (i - 1)) & 1u;
     const int corr = (cxi(j) > 0 ? cxm : (cxi(j) < 0 ? cxp : 0)) + (cyi(j) > 0 ? cym : (cyi(j) < 0 ? cyp : 0)) +
                      (czi(j) > 0 ? czm : (czi(j) < 0 ? czp : 0));
-    const T v = __ldg(src + (bb ? i * N + n : n + L.off[j] + corr));
+    const int k = bb ? i * N + n : n + L.off[j] + corr;
+    const T v = HC_IN(L.status, k, 19LL * N) ? __ldg(src + k) : T(0);
     if constexpr (MW) {
       const T cuw = T(cxi(i)) * ux + T(cyi(i)) * uy + T(czi(i)) * uz;
       f[j] = bb ? v - T(6.0 * wi(i)) * cuw : v;
@@ -225,7 +228,7 @@ __device__ __forceinline__ void pull_inline(const LbmView<T>& L, const T* __rest
 template <typename T>
 __device__ __forceinline__ void pull_interior(const LbmView<T>& L, const T* __restrict__ src, int n, T f[19]) {
 #pragma unroll
-  for (int j = 0; j < 19; ++j) f[j] = __ldg(src + n + L.off[j]);
+  for (int j = 0; j < 19; ++j) f[j] = HC_IN(L.status, n + L.off[j], 19 * L.N) ? __ldg(src + n + L.off[j]) : T(0);
 }
 
 // rhoBar = sum f, j = sum c f over the shifted populations, pair-wise
@@ -276,28 +279,29 @@ __device__ __forceinline__ void pull_rows(const LbmView<T>& L, const T* __restri
     if (used) {
       const int sy = cyi(j) > 0 ? nb.ym : (cyi(j) < 0 ? nb.yp : Y);
       const int sz = czi(j) > 0 ? nb.zm : (czi(j) < 0 ? nb.zp : Z);
-      buf[xdir_slot(j) * slot_stride + ty * rowlen + X] =
-          src[j * N + ((long long)X + (long long)L.nx * ((long long)sy + (long long)L.ny * sz))];
+      const long long k = j * N + ((long long)X + (long long)L.nx * ((long long)sy + (long long)L.ny * sz));
+      buf[xdir_slot(j) * slot_stride + ty * rowlen + X] = HC_IN(L.status, k, 19 * N) ? src[k] : T(0);
     }
   }
   __syncthreads();
   if (!need) return;
   const uint32_t cls = m >> NB_CLASS_SHIFT;
-  f[0] = src[n];
+  f[0] = HC_IN(L.status, n, N) ? src[n] : T(0);
 #pragma unroll
   for (int j = 1; j < 19; ++j) {
     const int i = oppi(j);
     if (m & (1u << (i - 1))) {
       const uint32_t c = wall_class(L, i, X, Y, Z, nb, cls);
       const T cuw = T(cxi(i)) * L.uw[c][0] + T(cyi(i)) * L.uw[c][1] + T(czi(i)) * L.uw[c][2];
-      f[j] = src[i * N + n] - T(6.0 * wi(i)) * cuw;
+      f[j] = (HC_IN(L.status, i * N + n, 19 * N) ? src[i * N + n] : T(0)) - T(6.0 * wi(i)) * cuw;
     } else if (cxi(j) != 0) {
       const int xs = cxi(j) > 0 ? nb.xm : nb.xp;
       f[j] = buf[xdir_slot(j) * slot_stride + ty * rowlen + xs];
     } else {
       const int sy = cyi(j) > 0 ? nb.ym : (cyi(j) < 0 ? nb.yp : Y);
       const int sz = czi(j) > 0 ? nb.zm : (czi(j) < 0 ? nb.zp : Z);
-      f[j] = src[j * N + ((long long)X + (long long)L.nx * ((long long)sy + (long long)L.ny * sz))];
+      const long long k = j * N + ((long long)X + (long long)L.nx * ((long long)sy + (long long)L.ny * sz));
+      f[j] = HC_IN(L.status, k, 19 * N) ? src[k] : T(0);
     }
   }
 }

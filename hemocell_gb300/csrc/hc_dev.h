@@ -66,6 +66,25 @@ struct LbmView {
 constexpr unsigned int STATUS_NONFINITE = 1u;
 constexpr unsigned int STATUS_CELL_DELETED = 2u;
 constexpr unsigned int STATUS_WAIT_TIMEOUT = 4u;
+// bounds-checked build only: an index outside its array was caught, and the
+// access was skipped (a load reads zero)
+constexpr unsigned int STATUS_INDEX_CHECK = 16u;
+
+// The bounds-checked build (-DHC_CHECKED, libhcgpu_checked.so): HC_IN(status,
+// i, n) compares index i with its array's length n before the access it
+// guards; out of bounds it sets STATUS_INDEX_CHECK and yields false, and the
+// caller skips the access, so nothing traps and the host reads the status.
+// In the product build HC_IN is the constant true and guards compile away.
+__device__ __forceinline__ bool index_ok(unsigned int* status, long long i, long long n) {
+  if (i >= 0 && i < n) return true;
+  atomicOr(status, STATUS_INDEX_CHECK);
+  return false;
+}
+#ifdef HC_CHECKED
+#define HC_IN(status, i, n) (::hcd::index_ok((status), (long long)(i), (long long)(n)))
+#else
+#define HC_IN(status, i, n) true
+#endif
 
 // Launch plan of the bulk-copy collide-stream kernel (k_collide_stream_bulk):
 // each CTA owns a slab of R whole x-rows and sweeps a chunk of zlen planes,

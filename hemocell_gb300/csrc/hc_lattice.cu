@@ -20,6 +20,7 @@ namespace hcd {
 template <typename T, typename Idx, bool KEEP = false>
 __device__ __forceinline__ void collide_store(const LbmView<T>& L, Idx n, int Z, const T f[19], T Fx, T Fy, T Fz) {
   const Idx N = (Idx)L.N;
+  if (!HC_IN(L.status, n, N) || !HC_IN(L.status, Z, L.nz)) return;
   uint64_t pol = 0;
   if constexpr (KEEP) pol = l2_policy_evict_last();
   T rhoBar, jx, jy, jz;

@@ -269,7 +269,8 @@ int hc_vertex_count(const hc_handle* h);         /* vertices in use; does not wa
  * collide-stream timed out (the step's results are then invalid and the
  * handle must be destroyed: copies may still have been in flight), bit3 a
  * lattice node held more repulsion candidates than its slots (pairs were
- * dropped) */
+ * dropped), bit4 (bounds-checked build libhcgpu_checked.so only) an index
+ * outside its array was caught and the access skipped */
 int hc_device_status(hc_handle* h, unsigned int* status);
 
 /* --- launch tuning (project autotuner; results cached on disk) */
