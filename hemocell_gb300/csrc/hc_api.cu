@@ -730,14 +730,17 @@ bool fusable(hc_handle* h) {
 }
 
 // Shared memory the force assembly of one cell type takes in a variant: the
-// staged variant when its face and edge terms fit kStagedMax (two CTAs per
-// SM), else the vertex-centric path it falls back to.
-constexpr size_t kStagedMax = 110 * 1024;
+// staged variant when its face and edge terms fit the staged maximum, else
+// the vertex-centric path it falls back to.  FP32: 110 KB, so that two CTAs
+// share an SM; FP64: 200 KB, since the FP64 kernel's registers (144 a thread
+// at 384 threads) already hold one CTA per SM, and an FP64 RBC's terms take
+// 150 KB.
+size_t staged_max(const hc_handle* h) { return (h->f64 ? 200 : 110) * (size_t)1024; }
 size_t mech_smem(const hc_handle* h, const TypeSlot& ts, int variant) {
   const size_t gather = h->f64 ? hcd::mechanics_smem_bytes<double>(ts.tc.nv) : hcd::mechanics_smem_bytes<float>(ts.tc.nv);
   if (variant != 2) return gather;
   const size_t staged = hcd::mechanics_staged_bytes(ts.tc.model, ts.tc.nv, ts.tc.nf, ts.tc.ne, h->f64);
-  return staged <= kStagedMax ? staged : gather;
+  return staged <= staged_max(h) ? staged : gather;
 }
 
 inline void prof_mark(hc_handle* h, int slot) {
