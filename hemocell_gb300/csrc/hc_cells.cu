@@ -31,7 +31,7 @@ __device__ __forceinline__ T tmax(T a, T b) {
 // fractional part once in double and the rest in float.
 template <typename T>
 struct Kern {
-  long long node[8];
+  int node[8];  // the lattice holds fewer than 2^31 nodes (hc_create's size limit)
   T w[8];
 };
 
@@ -80,8 +80,7 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
     if (idx[0][ax] < 0 || idx[1][ay] < 0 || idx[2][az] < 0) continue;
     const T w = phi[0][ax] * phi[1][ay] * phi[2][az];
     if (w == T(0)) continue;
-    const long long nd =
-        (long long)idx[0][ax] + (long long)L.nx * ((long long)idx[1][ay] + (long long)L.ny * idx[2][az]);
+    const int nd = idx[0][ax] + L.nx * (idx[1][ay] + L.ny * idx[2][az]);
     if (!HC_IN(L.status, nd, L.N) || L.flag[nd] != 0) continue;
     total += w;
     K.node[s] = nd;
