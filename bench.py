@@ -398,7 +398,7 @@ def serving_leg(args, fp64_pipe_mlups=None):
         return {k: v for k, v in d.items() if k != "results"}
 
     per_seed = {}
-    for seed in (1, 2, 3):
+    for seed in ((1, 2, 3) if args.serve_solo > 0 else ()):
         stream = S.request_stream(seed=seed, rate=200.0, count=10000)
         reqs = stream[:args.serve_solo]
         solves = {r.id: S.Solve(r) for r in reqs}        # geometry and packing, outside the clock
@@ -410,16 +410,24 @@ def serving_leg(args, fp64_pipe_mlups=None):
                                "batched_f64": trim(b64),
                                "speedup_f32_vs_solo": b32["solves_per_s"] / solo["solves_per_s"],
                                "speedup_f64_vs_solo": b64["solves_per_s"] / solo["solves_per_s"]}
-    stream = S.request_stream(seed=1, rate=200.0, count=10000)
-    head = stream[:args.serve_requests]
-    solves = {r.id: S.Solve(r) for r in head}
-    kw = dict(budget_bytes=budget, max_slots=64, chunk_steps=50, solves=solves)
-    sat32 = S.serve(head, L.HC_FORM_MIXED_F32, **kw)
-    rate_sub = 0.5 * sat32["solves_per_s"]
-    sub = S.with_arrivals(head[: max(8, args.serve_requests // 3)], rate_sub, seed=2)
-    sub32 = S.serve(sub, L.HC_FORM_MIXED_F32, **kw)
+    # the saturated FP32 stream of each seed asked for (the first n requests of
+    # the seed's 10,000), then the first seed's stream at half its capacity
+    seeds = [int(x) for x in str(args.serve_seeds).split(",") if x.strip()]
+    sat_by_seed, sub32, rate_sub = {}, None, None
+    for k, seed in enumerate(seeds):
+        stream = S.request_stream(seed=seed, rate=200.0, count=10000)
+        head = stream[:args.serve_requests]
+        solves = {r.id: S.Solve(r) for r in head}
+        kw = dict(budget_bytes=budget, max_slots=64, chunk_steps=50, solves=solves)
+        sat_by_seed[str(seed)] = trim(S.serve(head, L.HC_FORM_MIXED_F32, **kw))
+        if k == 0:
+            rate_sub = 0.5 * sat_by_seed[str(seed)]["solves_per_s"]
+            sub = S.with_arrivals(head[: max(8, args.serve_requests // 3)], rate_sub, seed=2)
+            sub32 = S.serve(sub, L.HC_FORM_MIXED_F32, **kw)
+        del solves, kw
     small = small_box_kernels()
-    geo = lambda k: math.exp(sum(math.log(per_seed[s][k]) for s in per_seed) / len(per_seed))
+    geo = lambda k: (math.exp(sum(math.log(per_seed[s][k]) for s in per_seed) / len(per_seed))
+                     if per_seed else None)
     out = {
         "workload": "independent sheared boxes, edge U{32,48,64,96}, 1-8 RBC (642 vertices), shear 50-500/s, "
                     "kLink/kBend x log-U(0.5,5), 500-5000 steps; Poisson arrivals at 200/s",
@@ -427,10 +435,12 @@ def serving_leg(args, fp64_pipe_mlups=None):
         "per_seed": per_seed,
         "speedup_f32_vs_solo_geomean": geo("speedup_f32_vs_solo"),
         "speedup_f64_vs_solo_geomean": geo("speedup_f64_vs_solo"),
-        "saturated_f32_200_per_s": trim(sat32),
-        "subsaturated_f32": dict(trim(sub32), offered_rate_target=rate_sub),
+        "saturated_f32_200_per_s": dict(sat_by_seed[str(seeds[0])], seed=seeds[0]),
+        "subsaturated_f32": dict(trim(sub32), offered_rate_target=rate_sub, seed=seeds[0]),
         "small_box": small,
     }
+    if len(seeds) > 1:
+        out["saturated_f32_by_seed"] = sat_by_seed
     if fp64_pipe_mlups:
         # the FP64 arithmetic bound: the pipe's FP64 form keeps the FP64 pipe
         # busy, so no mix of solves steps FP64 lattices much faster than that
@@ -499,6 +509,7 @@ def main():
     ap.add_argument("--no-kolmogorov", action="store_true", help="skip the 128^3 suspension leg")
     ap.add_argument("--no-mixed-error", action="store_true", help="skip the FP32-vs-FP64 error report")
     ap.add_argument("--serve-requests", type=int, default=96, help="requests of the saturated FP32 stream")
+    ap.add_argument("--serve-seeds", default="1", help="seeds of the saturated FP32 stream, comma-separated")
     ap.add_argument("--serve-solo", type=int, default=12, help="requests run one at a time (and batched) "
                                                                  "for the speed-up")
     args = ap.parse_args()
