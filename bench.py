@@ -450,6 +450,17 @@ def serving_leg(args, fp64_pipe_mlups=None):
     return out
 
 
+def step_kernel_names(tuning) -> dict:
+    """The FP32 kernels that the tuned batched step launches, by `hc_profile_kernels`' keys."""
+    kind = tuning[7] & 0xFF
+    cs = "k_collide_stream<float>" if kind == 0 else ("k_collide_stream_fluid<float>" if kind == 1
+                                                       else "k_collide_stream_bulk<float>")
+    nv = {0x000: "k_node_velocity<float>", 0x100: "k_node_velocity_fluid<float>",
+          0x200: "k_node_velocity_packed<float>", 0x300: "k_node_velocity_dense<float>"}[tuning[7] & 0x300]
+    mech = {1: "k_mechanics_scatter<float>", 2: "k_mechanics_staged<float>"}.get(tuning[6], "k_mechanics<float>")
+    return {"collide_stream": cs, "node_velocity": nv, "mechanics": mech}
+
+
 def pipe_config(case, nvertices: int) -> dict:
     """The `config` of both arms: the workload only (the arithmetic of each
     arm is in its top-level `form`)."""
@@ -554,8 +565,7 @@ def main():
     kernel_bytes = {"collide_stream": fluid * BYTES_NODE["f32"],
                     "node_velocity": fluid * BYTES_NODE_VELOCITY["f32"],
                     "mechanics": st.vertices * BYTES_VERTEX["f32"]}
-    kernel_names = {"collide_stream": "k_collide_stream<float>", "node_velocity": "k_node_velocity_dense<float>",
-                    "mechanics": "k_mechanics<float>"}
+    kernel_names = step_kernel_names(tuning)
     kernels = {}
     for k, b in kernel_bytes.items():
         gbs = b / (prof[k] * 1e-3) / 1e9
