@@ -709,16 +709,16 @@ __device__ __forceinline__ void spread_vertex(const MechView<T>& M, int gi, V3t<
 // phi2 weights, Euler step, nearest node and tile, and the cell's deletion
 // when a vertex reaches a wall node (core/hemoCellParticleField.cpp:566-588,
 // :819-839).
+// voff and alive are the cell's first vertex and its state before the step;
+// `hit` is a shared flag the caller cleared before its last barrier.  Returns
+// whether the cell is still alive; the deletion is written to the cell's state
+// by thread 0.  Ends with a barrier: every vertex is advanced and binned.
 template <typename T>
-__device__ __forceinline__ void advance_cell(const MechView<T>& M, const TypeDev& t, int cell) {
-  __shared__ int hit;
+__device__ __forceinline__ bool advance_cell(const MechView<T>& M, const TypeDev& t, int cell, int voff, bool alive,
+                                             int& hit) {
   const VertexView<T>& vv = M.vv;
   const LbmView<T>& L = M.L;
   const long long V = vv.V;
-  const int voff = M.cell_voff[cell];
-  if (threadIdx.x == 0) hit = 0;
-  __syncthreads();
-  const bool alive = vv.alive[cell] != 0;
   for (int k = threadIdx.x; k < t.nv; k += blockDim.x) {
     const int i = voff + k;
     if (!alive) {
@@ -776,28 +776,28 @@ __device__ __forceinline__ void advance_cell(const MechView<T>& M, const TypeDev
     if (L.flag[nd] != 0) hit = 1;
   }
   __syncthreads();
-  if (threadIdx.x == 0 && hit) {
+  const bool deleted = alive && hit;
+  if (threadIdx.x == 0 && deleted) {
     vv.alive[cell] = 0;
     atomicOr(vv.status, STATUS_CELL_DELETED);
   }
-  __syncthreads();
+  return alive && !deleted;
 }
 
 // The vertex-centric force assembly of one cell (variant 0; the staged
 // variant falls back to it for cell types too large for its shared memory).
 // sx holds 6 nv T + nv bytes of shared memory after `red` (34 doubles).
 template <typename T>
-__device__ __forceinline__ void gather_cell(const MechView<T>& M, const TypeDev& t, int cell, double* red, T* sx) {
+__device__ __forceinline__ void gather_cell(const MechView<T>& M, const TypeDev& t, int voff, bool alive, double* red,
+                                            T* sx) {
   const VertexView<T>& vv = M.vv;
   const long long V = vv.V;
   const int tid = threadIdx.x, bs = blockDim.x;
   constexpr bool kF64 = sizeof(T) == 8;
   const int nv = t.nv;
-  const int voff = M.cell_voff[cell];
   T* sbf = sx + 3 * nv;  // own bending force per vertex
   uint8_t* srn = reinterpret_cast<uint8_t*>(sbf + 3 * nv);  // valence per vertex
   if (!HC_IN(vv.status, (long long)voff + nv - 1, V)) return;  // the cell's vertices in the arrays
-  const bool alive = vv.alive[cell] != 0;
   for (int k = tid; k < nv; k += bs) srn[k] = (uint8_t)t.ring_n[k];
   // positions relative to the cell's vertex 0 (translation invariant forces;
   // the volume sum stays well conditioned far from the origin)
@@ -975,13 +975,20 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics(const 
   __shared__ TypeDev tshared;
   double* red = smem_d;  // 34 doubles
   T* sx = reinterpret_cast<T*>(smem_d + 34);
+  __shared__ int hit;
   for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
     const int cell = M.cells[ci];
     __syncthreads();  // previous cell fully written out
-    if (threadIdx.x == 0) tshared = M.types[M.cell_type[cell]];
+    if (threadIdx.x == 0) {
+      tshared = M.types[M.cell_type[cell]];
+      hit = 0;
+    }
+    // the cell's scalars load while thread 0 fetches the type
+    const int voff = M.cell_voff[cell];
+    bool alive = M.vv.alive[cell] != 0;
     __syncthreads();
-    if (M.fuse_advance) advance_cell(M, tshared, cell);
-    gather_cell(M, tshared, cell, red, sx);
+    if (M.fuse_advance) alive = advance_cell(M, tshared, cell, voff, alive, hit);
+    gather_cell(M, tshared, voff, alive, red, sx);
   }
   pdl_trigger();
 }
@@ -1014,15 +1021,21 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics_staged
   const long long V = vv.V;
   const int tid = threadIdx.x, bs = blockDim.x;
   constexpr bool kF64 = sizeof(T) == 8;
+  __shared__ int hit;
   for (int ci = blockIdx.x; ci < M.ncells; ci += gridDim.x) {
     const int cell = M.cells[ci];
     __syncthreads();
-    if (tid == 0) tshared = M.types[M.cell_type[cell]];
+    if (tid == 0) {
+      tshared = M.types[M.cell_type[cell]];
+      hit = 0;
+    }
+    const int voff = M.cell_voff[cell];
+    bool alive = vv.alive[cell] != 0;
     __syncthreads();
     const TypeDev& t = tshared;
-    if (M.fuse_advance) advance_cell(M, t, cell);
+    if (M.fuse_advance) alive = advance_cell(M, t, cell, voff, alive, hit);
     if (staged_smem_bytes<T>(t.model, t.nv, t.nf, t.ne) > (size_t)M.dyn_smem) {
-      gather_cell(M, t, cell, red, sx);
+      gather_cell(M, t, voff, alive, red, sx);
       continue;
     }
     const int nv = t.nv, nf = t.nf, ne = t.ne;
@@ -1032,8 +1045,6 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 384 : 768) k_mechanics_staged
     T* sedge = sface + 7 * nf;
     T* spltb = sedge + 3 * ne;
     uint8_t* srn = reinterpret_cast<uint8_t*>(spltb + (plt ? 3 * ne : 0));
-    const int voff = M.cell_voff[cell];
-    const bool alive = vv.alive[cell] != 0;
     const double r0x = vv.x[voff], r0y = vv.x[V + voff], r0z = vv.x[2 * V + voff];
     for (int k = tid; k < nv; k += bs) {
       srn[k] = (uint8_t)t.ring_n[k];
