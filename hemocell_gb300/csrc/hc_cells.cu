@@ -13,6 +13,7 @@
 
 #include "hc_async.cuh"
 #include "hc_d3q19.cuh"
+#include "hc_posbits.h"
 
 namespace hcd {
 
@@ -28,7 +29,8 @@ __device__ __forceinline__ T tmax(T a, T b) {
 // (x, y, z) order.  Nodes off a non-periodic axis, zero weights and boundary
 // nodes are skipped (slot node = -1); the weights are renormalised to one.
 // FP64 evaluates phi2(p - q) exactly as the reference; FP32 takes the
-// fractional part once in double and the rest in float.
+// fractional part (float)(p - floor(p)) once, from the bits of the FP64
+// coordinate (hc_posbits.h), and the rest in float.
 template <typename T>
 struct Kern {
   int node[8];  // the lattice holds fewer than 2^31 nodes (hc_create's size limit)
@@ -44,16 +46,27 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
   int idx[3][2];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    const double q0 = floor(P[a]);
+    long long qi;
     if (kF64) {
+      const double q0 = floor(P[a]);
       phi[a][0] = tmax(T(1) - T(fabs(P[a] - q0)), T(0));
       phi[a][1] = tmax(T(1) - T(fabs(P[a] - (q0 + 1.0))), T(0));
+      qi = (long long)q0;
     } else {
-      const T fr = (T)(P[a] - q0);  // in [0, 1)
-      phi[a][0] = T(1) - fr;
-      phi[a][1] = fr;
+      // floor(P) and the fraction (float)(P - floor(P)) from the bits of P,
+      // the FP64 instructions only outside [1, 2^31)
+      int qs, up;
+      float fs;
+      if (hcpos::split(P[a], qs, fs, up)) {
+        qi = qs;
+      } else {
+        const double q0 = floor(P[a]);
+        fs = (float)(P[a] - q0);
+        qi = (long long)q0;
+      }
+      phi[a][0] = T(1) - (T)fs;
+      phi[a][1] = (T)fs;
     }
-    const long long qi = (long long)q0;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const long long q = qi + k;
@@ -462,7 +475,7 @@ __global__ void __launch_bounds__(256) k_interp_advance(const LbmView<T> L, cons
   bool inside = true;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    long long qi = (long long)floor(P[a] + 0.5);
+    long long qi = hcpos::nearest(P[a]);  // floor(P + 0.5), exactly
     if (qi < 0 || qi >= dims[a]) {
       if (L.per[a]) {
         long long mm = qi % dims[a];
@@ -754,7 +767,7 @@ __device__ __forceinline__ bool advance_cell(const MechView<T>& M, const TypeDev
     int q[3];
     bool inside = true;
     for (int a = 0; a < 3; ++a) {
-      long long qi = (long long)floor(P[a] + 0.5);
+      long long qi = hcpos::nearest(P[a]);  // floor(P + 0.5), exactly
       if (qi < 0 || qi >= dims[a]) {
         if (L.per[a]) {
           const long long mm = qi % dims[a];
@@ -1458,7 +1471,7 @@ __global__ void k_bin_vertices(const LbmView<T> L, const VertexView<T> vv, const
   bool inside = vv.alive[vv.vcell[i]] != 0;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    long long qi = (long long)floor(P[a] + 0.5);
+    long long qi = hcpos::nearest(P[a]);  // floor(P + 0.5), exactly
     if (qi < 0 || qi >= dims[a]) {
       if (L.per[a]) {
         long long mm = qi % dims[a];
