@@ -66,6 +66,11 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
       }
       phi[a][0] = T(1) - (T)fs;
       phi[a][1] = (T)fs;
+      // a fraction within 2^-25 of one rounds to 1.0f; the lower node's
+      // weight is then the rounded exact complement 1 - (P - floor(P)) (exact
+      // in FP64), not zero, so that a vertex next to a wall keeps the FP64
+      // form's renormalised stencil
+      if (fs == 1.0f) phi[a][0] = (T)(1.0 - (P[a] - (double)qi));
     }
 #pragma unroll
     for (int k = 0; k < 2; ++k) {

@@ -266,6 +266,80 @@ def test_advance_and_bins_bit_exact(built):
     hc.close()
 
 
+def _edge_coordinates(case, x, rng):
+    """Vertex coordinates on the cases the mixed form's integer split of an
+    FP64 coordinate must get right: integers, half-integers (floor(P + 0.5)
+    ties), one ulp either side of each, and on periodic axes values below 1,
+    exactly 0 and negative (the FP64 fallback)."""
+    x = x.copy()
+    idx = rng.permutation(len(x))
+    edge = idx[: len(x) // 2]
+    for k, i in enumerate(edge):
+        a = k % 3
+        base = float(np.floor(x[i, a]))
+        kind = (k // 3) % 8
+        if kind == 0:
+            val = base + 0.5
+        elif kind == 1:
+            val = np.nextafter(base + 0.5, -np.inf)
+        elif kind == 2:
+            val = np.nextafter(base + 0.5, np.inf)
+        elif kind == 3:
+            val = base
+        elif kind == 4:
+            val = np.nextafter(base, np.inf)
+        elif kind == 5:
+            val = np.nextafter(base + 1.0, -np.inf)
+        elif case.periodic[a]:
+            val = (-0.3, 0.0, 0.5, 0.999999999999)[k % 4] if kind == 6 else -1.0 + (k % 5) * 0.25
+        else:
+            val = base + 0.25
+        x[i, a] = val
+    return x, edge
+
+
+@pytest.mark.parametrize("wall", [False, True])
+def test_stencil_edge_coordinates_fp32(built, wall):
+    """The mixed form takes the stencil's base node and fractions, and each
+    vertex's nearest node, from the bits of the FP64 position (FP64
+    instructions below 1, for negative and non-finite coordinates).  On edge
+    coordinates the spread and the interpolation match the FP64 oracle at the
+    form's FP32 rounding, and the advance's positions, bins and cell states
+    are bit-exact (velocities exactly representable in FP32, zero on the
+    edge vertices, so x + v is the same double on both sides)."""
+    from hemocell_gb300 import _lib as L
+    case = mixed_box(wall=wall)
+    hc = case.build(form=L.HC_FORM_MIXED_F32)
+    o = _orc().apply_case(case)
+    rng = np.random.default_rng(21)
+    _, _, x, v, fv = randomize(case, hc, o)
+    x, edge = _edge_coordinates(case, x, rng)
+    v = v.astype(np.float32).astype(np.float64)
+    v[edge] = 0.0
+    fv = fv.astype(np.float32).astype(np.float64)
+    hc.write_vertices(x, v, fv)
+    o.write_vertices(x, v, fv)
+    hc.stage(0)
+    o.stage("spread")
+    assert rel_l2(hc.read_force_field(0), o.read_force_field(0)) < 1e-5
+    hc.stage(2)
+    o.stage("interpolate")
+    assert rel_l2(hc.read_vertices()[1], o.read_vertices()[1]) < 1e-5
+    # the advance from exactly representable velocities
+    hc.write_vertices(x, v, None)
+    o.write_vertices(x, v, None)
+    hc.stage(3)
+    o.stage("advance")
+    assert np.array_equal(hc.read_vertices()[0], o.read_vertices()[0])
+    assert np.array_equal(hc.read_cells()[0], o.read_cells()[0])
+    bg = hc.read_bins()
+    bo = o.bins((8, 8, 8), None, case.dims)
+    for k in bo:
+        assert np.array_equal(bg[k], bo[k]), k
+    assert hc.device_status() & 5 == 0
+    hc.close()
+
+
 @pytest.mark.parametrize("which", ["walls", "periodic", "suspension"])
 def test_neighbour_lists_bit_exact(built, which):
     """hc_read_neighbours (per tile, the cells of the tile and its 26
