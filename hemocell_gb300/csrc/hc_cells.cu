@@ -55,22 +55,23 @@ __device__ __forceinline__ void ibm_weights(const LbmView<T>& L, double px, doub
     } else {
       // floor(P) and the fraction (float)(P - floor(P)) from the bits of P,
       // the FP64 instructions only outside [1, 2^31)
-      int qs, up;
-      float fs;
-      if (hcpos::split(P[a], qs, fs, up)) {
+      // A fraction within 2^-25 of one rounds to 1.0f; the lower node's
+      // weight is then the rounded exact complement 1 - (P - floor(P)), not
+      // zero, so that a vertex next to a wall keeps the FP64 form's
+      // renormalised stencil.
+      int qs;
+      float w0, w1;
+      if (hcpos::split_weights(P[a], qs, w0, w1)) {
         qi = qs;
       } else {
         const double q0 = floor(P[a]);
-        fs = (float)(P[a] - q0);
+        const double fr = P[a] - q0;  // exact, as is 1 - fr
+        w1 = (float)fr;
+        w0 = w1 == 1.0f ? (float)(1.0 - fr) : 1.0f - w1;
         qi = (long long)q0;
       }
-      phi[a][0] = T(1) - (T)fs;
-      phi[a][1] = (T)fs;
-      // a fraction within 2^-25 of one rounds to 1.0f; the lower node's
-      // weight is then the rounded exact complement 1 - (P - floor(P)) (exact
-      // in FP64), not zero, so that a vertex next to a wall keeps the FP64
-      // form's renormalised stencil
-      if (fs == 1.0f) phi[a][0] = (T)(1.0 - (P[a] - (double)qi));
+      phi[a][0] = (T)w0;
+      phi[a][1] = (T)w1;
     }
 #pragma unroll
     for (int k = 0; k < 2; ++k) {

@@ -31,7 +31,7 @@ static uint32_t fbits(float f) {
   return b;
 }
 
-static long long cases = 0;
+static long long cases = 0, rounded_to_one = 0;
 
 static bool check(double P) {
   ++cases;
@@ -57,6 +57,21 @@ static bool check(double P) {
            (double)fr_ref, fbits(fr), fbits(fr_ref), up, near);
     return false;
   }
+  // the stencil weights: w1 = the rounded fraction, w0 = 1 - w1 or, when the
+  // fraction rounds to one, the rounded exact complement
+  int qw = 0;
+  float w0 = 0.f, w1 = 0.f;
+  if (!hcpos::split_weights(P, qw, w0, w1)) {
+    printf("split_weights refused P=%.17g\n", P);
+    return false;
+  }
+  const float w0_ref = fr_ref == 1.0f ? (float)(1.0 - (P - q0)) : 1.0f - fr_ref;
+  if (qw != q || fbits(w1) != fbits(fr_ref) || fbits(w0) != fbits(w0_ref)) {
+    printf("weights P=%.17g: w0 %.9g/%.9g w1 %.9g/%.9g\n", P, (double)w0, (double)w0_ref, (double)w1,
+           (double)fr_ref);
+    return false;
+  }
+  if (fr_ref == 1.0f) ++rounded_to_one;
   return true;
 }
 
@@ -109,6 +124,10 @@ int main() {
                             std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::denorm_min()};
   for (double P : refused)
     if (!check(P)) return 1;
+  if (rounded_to_one < 1000) {
+    printf("only %lld fractions rounded to one\n", rounded_to_one);
+    return 1;
+  }
   printf("ok %lld\n", cases);
   return 0;
 }
