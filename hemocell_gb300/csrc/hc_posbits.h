@@ -6,8 +6,8 @@
 // operations per axis, and this GPU's FP64 pipe takes 16 SM cycles per warp
 // instruction.  The same results follow exactly from the IEEE-754 fields of P
 // with 32-bit integer operations and one 32-bit conversion:
-//   for 1 <= P < 2^31, P = m * 2^-s with m the 53-bit significand and
-//   s = 52 - e in [22, 52];
+//   for 1 <= P < 2^20, P = m * 2^-s with m the 53-bit significand and
+//   s = 52 - e in [33, 52];
 //   floor(P) = m >> s, and the fraction is F * 2^-s with F = m mod 2^s;
 //   P - floor(P) is exact in FP64 (Sterbenz), so its conversion to float is F
 //   rounded to 24 significant bits, to nearest, ties to even: F's leading 32
@@ -15,9 +15,9 @@
 //   floor(P + 0.5) = floor(P) + (F >= 2^(s-1)): P + 0.5 is exact in FP64 for
 //   these P, or rounds within [2^(e+1), 2^(e+1) + 0.5) when it crosses the
 //   binade, which has the same floor.
-// Outside [1, 2^31) (negative coordinates on a periodic axis, the first unit
-// interval, non-finite values) split() returns false and the caller takes the
-// FP64 instructions.  Host and device compile the same code; a CPU test
+// Outside [1, 2^20) (negative coordinates on a periodic axis, the first unit
+// interval, coordinates beyond a million nodes, non-finite values) split()
+// returns false and the caller takes the FP64 instructions.  Host and device compile the same code; a CPU test
 // compares it bit for bit with the FP64 operations.
 #pragma once
 #include <math.h>
@@ -82,9 +82,10 @@ HC_POS_HD float uint_to_float_rn(uint32_t x) {
 // 2^k as a float, -126 <= k <= 127
 HC_POS_HD float pow2f(int k) { return float_from_bits((uint32_t)(k + 127) << 23); }
 
-// The fields of a coordinate 1 <= P < 2^31: floor q, the fraction F * 2^-s
-// with F = fh:fl (s = 22..52 fraction bits), and up = 1 when the fraction is
-// at least 0.5.  Returns false for every other P.
+// The fields of a coordinate 1 <= P < 2^20 (every lattice coordinate in
+// practice): floor q, the fraction F * 2^-s with F = fh:fl (s = 33..52
+// fraction bits, so fh holds the top s - 32 of them), and up = 1 when the
+// fraction is at least 0.5.  Returns false for every other P.
 struct FractionBits {
   int q, s, up;
   uint32_t fh, fl;
@@ -93,37 +94,27 @@ HC_POS_HD bool fraction_bits(double P, FractionBits& b) {
   uint32_t hi, lo;
   double_words(P, hi, lo);
   const int be = (int)(hi >> 20);  // sign bit and biased exponent
-  if ((unsigned)(be - 1023) > 30u) return false;
-  b.s = 1075 - be;                                  // fraction bits, 22..52
+  if ((unsigned)(be - 1023) > 19u) return false;
+  b.s = 1075 - be;                                  // fraction bits, 33..52
+  const int t = b.s - 32;                           // fraction bits in the high word, 1..20
   const uint32_t mh = (hi & 0xFFFFFu) | 0x100000u;  // significand bits 32..52
-  if (b.s >= 32) {
-    const int t = b.s - 32;  // 0..20
-    b.q = (int)(mh >> t);
-    b.fh = mh & ((1u << t) - 1u);
-    b.fl = lo;
-    b.up = (int)((t > 0 ? (b.fh >> (t - 1)) : (b.fl >> 31)) & 1u);
-  } else {
-    b.q = (int)((mh << (32 - b.s)) | (lo >> b.s));
-    b.fh = 0u;
-    b.fl = lo & ((1u << b.s) - 1u);
-    b.up = (int)((b.fl >> (b.s - 1)) & 1u);
-  }
+  b.q = (int)(mh >> t);
+  b.fh = mh & ((1u << t) - 1u);
+  b.fl = lo;
+  b.up = (int)((b.fh >> (t - 1)) & 1u);
   return true;
 }
 
-// The fraction rounded to float, to nearest, ties to even.
+// The fraction rounded to float, to nearest, ties to even: F's leading 32
+// bits (all of F when fh is zero) with a sticky bit for the rest.
 HC_POS_HD float fraction_to_float(const FractionBits& b) {
-  if (b.fh != 0u) {
-    // F has 33..52 bits: its leading 32 bits, with a sticky bit for the rest
-    const int n = 32 - leading_zeros32(b.fh);  // bits of fh, 1..20
-    uint32_t top = shift_right_pair(b.fl, b.fh, n);
-    if (b.fl & ((1u << n) - 1u)) top |= 1u;
-    return uint_to_float_rn(top) * pow2f(n - b.s);
-  }
-  return uint_to_float_rn(b.fl) * pow2f(-b.s);
+  const int n = 32 - leading_zeros32(b.fh);  // bits of fh, 0..20
+  uint32_t top = shift_right_pair(b.fl, b.fh, n);
+  if (b.fl & ((1u << n) - 1u)) top |= 1u;
+  return uint_to_float_rn(top) * pow2f(n - b.s);
 }
 
-// For 1 <= P < 2^31: q = floor(P), fr = (float)(P - floor(P)) rounded as the
+// For 1 <= P < 2^20: q = floor(P), fr = (float)(P - floor(P)) rounded as the
 // FP64 conversion rounds it, up = 1 when P - floor(P) >= 0.5 (so that
 // floor(P + 0.5) = q + up).  Returns false, leaving the outputs unset, for
 // every other P.
@@ -137,16 +128,17 @@ HC_POS_HD bool split(double P, int& q, float& fr, int& up) {
 }
 
 // The two linear weights of the mixed form's stencil along one axis, for
-// 1 <= P < 2^31: w1 = (float)(P - floor(P)) and w0 = 1 - w1, except when the
+// 1 <= P < 2^20: w1 = (float)(P - floor(P)) and w0 = 1 - w1, except when the
 // fraction rounds to 1: w0 is then the rounded exact complement
 // 1 - (P - floor(P)) = (2^s - F) * 2^-s, not zero (2^s - F < 2^(s-24) then
-// fits 32 bits).  Returns false for every other P.
+// fits 32 bits, and is -fl modulo 2^32 since s >= 32).  Returns false for
+// every other P.
 HC_POS_HD bool split_weights(double P, int& q, float& w0, float& w1) {
   FractionBits b;
   if (!fraction_bits(P, b)) return false;
   q = b.q;
   w1 = fraction_to_float(b);
-  const uint32_t g = b.s >= 32 ? 0u - b.fl : (1u << b.s) - b.fl;
+  const uint32_t g = 0u - b.fl;
   w0 = w1 == 1.0f ? uint_to_float_rn(g) * pow2f(-b.s) : 1.0f - w1;
   return true;
 }
